@@ -1,0 +1,186 @@
+/*
+ * fock_gb300.h -- C ABI of the GB300 Fock-basis circuit simulator.
+ *
+ * Plain C: device pointers are `void*` / `double*` into GPU memory, host
+ * pointers are marked "host", streams are `cudaStream_t` passed as `void*`
+ * (NULL = legacy default stream).  Every entry point returns FOCK_OK (0) or a
+ * negative status; `fock_last_error` returns the message of the last failure
+ * on the calling thread.  No entry point allocates device memory: callers pass
+ * every state buffer and workspace (sizes from the *_bytes queries).
+ *
+ * States (layout of strawberryfields/backends/fockbackend/backend.py:50-56):
+ * a pure n-mode state is a C-order tensor [D]^n (mode 0 slowest); a mixed
+ * state is [D]^(2n) with interleaved (ket, bra) axes.  dtype FOCK_C64 stores
+ * interleaved float pairs (complex64), FOCK_C128 double pairs (complex128).
+ * Gate matrices are always built on the device in FP64.
+ *
+ * Each entry point cites the reference interface it replaces (paths relative
+ * to the Strawberry Fields source tree).
+ */
+#ifndef FOCK_GB300_H
+#define FOCK_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FOCK_OK 0
+#define FOCK_ERR_INVALID (-1)     /* bad argument (Python: ValueError) */
+#define FOCK_ERR_CUDA (-2)        /* CUDA runtime error */
+#define FOCK_ERR_UNSUPPORTED (-3) /* valid request this build does not implement (NotImplementedError) */
+
+/* state precision */
+#define FOCK_C64 0
+#define FOCK_C128 1
+
+/* gate kinds (names follow strawberryfields/backends/base.py) */
+#define FOCK_ROTATION 1          /* R(phi) = exp(i phi n)            base.py:301  */
+#define FOCK_KERR 2              /* K(kappa) = exp(i kappa n^2)       base.py:583  */
+#define FOCK_DISPLACEMENT 3      /* D(r e^{i phi})                    base.py:310  */
+#define FOCK_SQUEEZE 4           /* S(r e^{i phi})                    base.py:320  */
+#define FOCK_BEAMSPLITTER 5      /* BS(theta, phi)                    base.py:330  */
+#define FOCK_TWO_MODE_SQUEEZE 6  /* S2(r e^{i phi})                   base.py:602  */
+#define FOCK_MZGATE 7            /* MZ(phi_in, phi_ex)                base.py:341  */
+#define FOCK_CROSS_KERR 8        /* CK(kappa) = exp(i kappa n1 n2)    base.py:592  */
+#define FOCK_LOSS 9              /* loss channel N(T) (mixed states)  base.py:352  */
+
+/* One gate of a circuit.  Parameters live in a device array `params`;
+ * p0 = params[pidx], p1 = params[pidx + 1] (two-parameter gates). */
+typedef struct fock_gate {
+  int32_t kind;
+  int32_t mode1;
+  int32_t mode2; /* -1 for single-mode gates */
+  int32_t pidx;
+} fock_gate;
+
+/* ---------------------------------------------------------------- errors */
+int fock_last_error(char* buf, size_t len);
+int fock_version(void);
+
+/* ------------------------------------------------------- gate matrices (G1-G5)
+ * Number of complex entries of the matrix `fock_gate_matrix` writes:
+ * D*D for single-mode kinds, D(2D^2+1)/3 (photon-number blocks) for two-mode
+ * kinds, 0 for unknown kinds.  Replaces the builders of
+ * strawberryfields/backends/fockbackend/ops.py: displacement :219,
+ * squeezing :238, two_mode_squeeze :257, kerr :274, cross_kerr :284,
+ * phase :309, beamsplitter :318, mzgate :332, lossChannel :471. */
+int64_t fock_gate_matrix_entries(int kind, int cutoff);
+/* Device workspace (bytes) the builder needs for one gate. */
+int64_t fock_gate_workspace_bytes(int kind, int cutoff);
+/* Build one gate matrix in FP64 on the device: `out` (device, complex128,
+ * fock_gate_matrix_entries entries) and, when `dout` is non-NULL, the
+ * derivative with respect to p0 (r or theta).  Single-mode kinds are
+ * row-major [out][in]; two-mode kinds are stored as photon-number blocks
+ * (see fock_expand_blocks).  Loss stores the superoperator on a (ket, bra)
+ * axis pair in difference-conserving blocks. */
+int fock_gate_matrix(int kind, double p0, double p1, int cutoff, void* out, void* dout,
+                     void* workspace, void* stream);
+/* Expand block storage to a dense [out1][in1][out2][in2] tensor of D^4
+ * complex128 entries (the index order of fockbackend/ops.py:329). */
+int fock_expand_blocks(int kind, int cutoff, const void* blocks, void* dense, void* stream);
+
+/* ------------------------------------------------------- state updates (K1-K6)
+ * Apply one gate to `in`, writing `out` (in != out).  Mixed states need
+ * `tmp` (a third state-sized buffer; NULL for pure states).
+ * `workspace`: fock_gate_workspace_bytes(kind, cutoff) bytes.
+ * `pre` (host, 4 doubles {theta1, kappa1, theta2, kappa2}, or NULL) are
+ * rotation angles and Kerr strengths applied to mode1/mode2 BEFORE the gate,
+ * i.e. exp(i (theta n + kappa n^2)): pending rotation/Kerr gates are folded
+ * into the next gate on the same mode this way.  Rotation, Kerr and
+ * cross-Kerr kinds run as one diagonal phase pass.
+ * Replaces Circuit.apply_gate_BLAS (fockbackend/circuit.py:118),
+ * apply_twomode_gate (:219), _apply_two_mode_passive (:307), _apply_S2 (:338)
+ * and _apply_channel for the loss channel (:65). */
+int fock_apply_gate(int kind, double p0, double p1, int mode1, int mode2,
+                    int num_modes, int cutoff, int pure, int dtype, const double* pre,
+                    const void* in, void* out, void* tmp, void* workspace, void* stream);
+/* Apply a caller-built single-mode matrix (device, complex128, D*D row-major)
+ * to one mode (e.g. cubic phase, fockbackend/circuit.py:590). */
+int fock_apply_matrix1(const void* mat, int mode, int num_modes, int cutoff, int pure, int dtype,
+                       const void* in, void* out, void* tmp, void* stream);
+/* Diagonal phases: multiply every amplitude by
+ * exp(i (sum_m angles[m*D + n_m] + sum_k ck_kappa[k] n_{a_k} n_{b_k}))
+ * (bra side conjugated for mixed states).  `angles` device (num_modes*D) or
+ * NULL; ck_modes/ck_kappa host arrays of n_ck <= 32 pairs.  Rotation,
+ * Kerr and cross-Kerr of fockbackend/circuit.py:155-177 (diagonal path). */
+int fock_apply_phases(int num_modes, int cutoff, int pure, int dtype, const double* angles,
+                      int n_ck, const int* ck_modes, const double* ck_kappa,
+                      const void* in, void* out, void* stream);
+/* rho = |psi><psi| with interleaved axes (fockbackend/ops.py:110 mix). */
+int fock_mix(int num_modes, int cutoff, int dtype, const void* ket, void* dm, void* stream);
+/* Vacuum state (fockbackend/ops.py:363,373). */
+int fock_vacuum(int num_modes, int cutoff, int pure, int dtype, void* state, void* stream);
+/* Replace the modes in `modes` (host, n_sub entries, any order) of a mixed
+ * state by the mixed state `sub` (device, complex128 [D]^(2 n_sub),
+ * interleaved): out = tr_modes(in) (x) sub, re-ordered so sub's k-th mode
+ * lands on modes[k] (fockbackend/circuit.py:393 prepare_multimode). */
+int fock_prepare_modes(int num_modes, int cutoff, int dtype, int n_sub, const int* modes,
+                       const void* sub, const void* in, void* out, void* workspace, void* stream);
+int64_t fock_prepare_workspace_bytes(int num_modes, int cutoff, int dtype, int n_sub);
+
+/* ------------------------------------------------------------ readouts (R1-R3)
+ * probs: |psi|^2 (pure) or diag(rho) (mixed), D^n doubles
+ * (states.py:580 all_fock_probs). */
+int fock_probs(int num_modes, int cutoff, int pure, int dtype, const void* state, double* probs,
+               void* stream);
+/* Photon-number distribution of every mode: out[m*D + k] = P(n_m = k), from
+ * one pass over the state (states.py:657 mean_photon without forming the full
+ * density matrix).  `workspace`: fock_marginals_workspace_bytes bytes. */
+int fock_marginals(int num_modes, int cutoff, int pure, int dtype, const void* state,
+                   double* out, void* workspace, void* stream);
+int64_t fock_marginals_workspace_bytes(int num_modes, int cutoff, int pure, int dtype);
+/* Single-mode reduced density matrix (complex128 D*D) of `mode`
+ * (states.py:613 reduced_dm, fockbackend/backend.py:209 state(modes)). */
+int fock_reduced_dm1(int num_modes, int cutoff, int pure, int dtype, int mode, const void* state,
+                     void* out, void* workspace, void* stream);
+int64_t fock_reduced_dm1_workspace_bytes(int num_modes, int cutoff, int pure, int dtype);
+
+/* ---------------------------------------------- compiled circuits + adjoint (A1-A3)
+ * A plan is a gate list compiled on the host: rotation/Kerr/cross-Kerr gates
+ * are fused into the neighbouring non-diagonal gate, so the state crosses HBM
+ * once per remaining op.  Forward: states[k] = op_k(states[k-1]) for the
+ * n_ops fused ops (states[-1] = `state_in`); with store_all = 0 only two
+ * slots are used (ping-pong).  Backward: the adjoint sweep of the gradient
+ * contract of strawberryfields/backends/tfbackend/ops.py:190-454 (custom
+ * gradients) and :688-854 (state contractions): given grad_state = dL/dpsi of
+ * the final state (torch convention dL/dRe + i dL/dIm), accumulate dL/dparams
+ * (device doubles, zeroed by the call) and leave dL/dpsi_in in grad_state. */
+typedef struct fock_plan fock_plan;
+typedef struct fock_plan_info {
+  int32_t n_ops;            /* fused ops */
+  int32_t n_gates;          /* gates in the list */
+  int64_t state_elems;      /* complex entries per state */
+  int64_t state_bytes;
+  int64_t workspace_bytes;  /* for forward and backward */
+  int64_t flops_fwd;        /* real flops of one forward */
+  int64_t bytes_fwd;        /* algorithmic HBM bytes of one forward (2 S per op) */
+} fock_plan_info;
+
+int fock_plan_create(int num_modes, int cutoff, int pure, int dtype, const fock_gate* gates,
+                     int n_gates, int n_params, fock_plan** out);
+void fock_plan_destroy(fock_plan* plan);
+int fock_plan_get_info(const fock_plan* plan, fock_plan_info* info);
+/* Fused op k: kind code (1 dense single-mode, 2 number-sum block, 3
+ * number-difference block), modes, number of gates fused into it. */
+int fock_plan_op(const fock_plan* plan, int k, int* kind, int* mode1, int* mode2, int* n_fused);
+int fock_plan_forward(fock_plan* plan, const double* params, const void* state_in, void* states,
+                      int store_all, void* workspace, void* stream);
+int fock_plan_backward(fock_plan* plan, const double* params, const void* state_in,
+                       const void* states, void* grad_state, void* grad_tmp, double* grad_params,
+                       void* workspace, void* stream);
+
+/* Per-op device timing of plan sweeps (CUDA events recorded between the op
+ * launches on the sweep's stream).  After enabling, every forward/backward
+ * call records; fock_plan_op_times reads the last sweep of each direction
+ * (milliseconds per op, op order) once the stream has completed. */
+int fock_plan_enable_timing(fock_plan* plan, int enable);
+int fock_plan_op_times(fock_plan* plan, float* fwd_ms, float* bwd_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FOCK_GB300_H */

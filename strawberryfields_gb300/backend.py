@@ -1,0 +1,270 @@
+"""``fock_gb300``: a Strawberry Fields ``BaseFock`` backend on one GB300 GPU.
+
+Same method names, argument meaning and exceptions as the reference's
+``FockBackend`` (``strawberryfields/backends/fockbackend/backend.py:29-329``,
+interface ``strawberryfields/backends/base.py:117-626``), so an unchanged
+``sf.Engine`` program runs on it::
+
+    import strawberryfields as sf
+    from strawberryfields_gb300 import sf_backend
+    eng = sf.Engine(sf_backend(), backend_options={"cutoff_dim": 12})
+
+``sf_backend()`` returns an instance of a subclass of the installed
+``BaseFock`` (required by ``BaseEngine.__init__``, engine.py:74-76); the
+plain :class:`FockGB300Backend` works without Strawberry Fields installed.
+Extra ``backend_options``: ``dtype`` (``"complex128"``, the reference's
+precision and the default, or ``"complex64"``) and ``device``.
+"""
+
+import string
+
+import numpy as np
+import torch
+
+from .circuit import DeviceCircuit
+from .states import FockStateGB300
+
+indices = string.ascii_lowercase
+
+
+class ModeMap:
+    """Map from external mode indices to internal ones; deleted modes map to
+    None (same behaviour as ``ModeMap`` in strawberryfields/backends/base.py:27)."""
+
+    def __init__(self, num_subsystems):
+        self._init = num_subsystems
+        self._map = list(range(num_subsystems))
+
+    def reset(self):
+        self._map = list(range(self._init))
+
+    def _ok(self, mode):
+        return mode is not None and 0 <= mode < len(self._map)
+
+    def remap(self, modes):
+        if isinstance(modes, int):
+            return self._map[modes]
+        return [self._map[m] for m in modes]
+
+    def valid(self, modes):
+        if modes is None:
+            return False
+        if isinstance(modes, int):
+            modes = [modes]
+        if len(modes) == 0 or len(modes) > len(self._map):
+            return False
+        return all(self._ok(m) for m in modes)
+
+    def show(self):
+        return self._map
+
+    def delete(self, modes):
+        if isinstance(modes, int):
+            modes = [modes]
+        if not self.valid(modes):
+            raise ValueError("Specified modes for deleting are invalid.")
+        new, ctr = [], 0
+        for m in range(len(self._map)):
+            if m in modes or self._map[m] is None:
+                new.append(None)
+            else:
+                new.append(ctr)
+                ctr += 1
+        self._map = new
+
+    def add(self, num_modes):
+        active = len([m for m in self._map if m is not None])
+        self._map += list(range(active, active + num_modes))
+
+
+class FockGB300Backend:
+    """GB300-native Fock backend (see module docstring)."""
+
+    short_name = "fock_gb300"
+    circuit_spec = "fock"
+    compiler = "fock"
+
+    def __init__(self):
+        self._supported = {"mixed_states": True, "fock_basis": True}
+        self._init_modes = None
+        self._modemap = None
+        self.circuit = None
+        self._options = {}
+
+    def __str__(self):
+        return self.__class__.__name__
+
+    def supports(self, name):
+        return self._supported.get(name, False)
+
+    # ----------------------------------------------------------------- modes
+    def _remap_modes(self, modes):
+        if isinstance(modes, int):
+            modes = [modes]
+            was_int = True
+        else:
+            was_int = False
+        map_ = self._modemap.show()
+        if not self._modemap.valid(modes) or None in [map_[m] for m in modes]:
+            raise ValueError("The specified modes are not valid.")
+        remapped = self._modemap.remap(modes)
+        return remapped[0] if was_int else remapped
+
+    def begin_circuit(self, num_subsystems, **kwargs):
+        cutoff_dim = kwargs.get("cutoff_dim", None)
+        pure = kwargs.get("pure", True)
+        if cutoff_dim is None:
+            raise ValueError("Argument 'cutoff_dim' must be passed to the Fock backend")
+        if not isinstance(cutoff_dim, int):
+            raise ValueError("Argument 'cutoff_dim' must be a positive integer")
+        if not isinstance(num_subsystems, int):
+            raise ValueError("Argument 'num_subsystems' must be a positive integer")
+        if not isinstance(pure, bool):
+            raise ValueError("Argument 'pure' must be either True or False")
+        dtype = kwargs.get("dtype", "complex128")
+        if dtype in (np.complex64, torch.complex64):
+            dtype = "complex64"
+        if dtype in (np.complex128, torch.complex128):
+            dtype = "complex128"
+        self._options = {"dtype": dtype, "device": kwargs.get("device", None)}
+        self._init_modes = num_subsystems
+        self.circuit = DeviceCircuit(num_subsystems, cutoff_dim, pure, dtype=dtype,
+                                     device=self._options["device"])
+        self._modemap = ModeMap(num_subsystems)
+
+    def add_mode(self, n=1, **kwargs):
+        raise NotImplementedError("fock_gb300 does not add modes after begin_circuit")
+
+    def del_mode(self, modes):
+        raise NotImplementedError("fock_gb300 does not delete modes")
+
+    def get_modes(self):
+        return [i for i, j in enumerate(self._modemap._map) if j is not None]
+
+    def reset(self, pure=True, **kwargs):
+        cutoff = kwargs.get("cutoff_dim", self.circuit._trunc)
+        self._modemap.reset()
+        self.circuit.reset(pure, num_subsystems=self._init_modes, cutoff_dim=cutoff)
+
+    def get_cutoff_dim(self):
+        return self.circuit._trunc
+
+    # ----------------------------------------------------------------- preparations
+    def prepare_vacuum_state(self, mode):
+        self.circuit.prepare_mode_fock(0, self._remap_modes(mode))
+
+    def prepare_coherent_state(self, r, phi, mode):
+        self.circuit.prepare_mode_coherent(r, phi, self._remap_modes(mode))
+
+    def prepare_squeezed_state(self, r, phi, mode):
+        self.circuit.prepare_mode_squeezed(r, phi, self._remap_modes(mode))
+
+    def prepare_displaced_squeezed_state(self, r_d, phi_d, r_s, phi_s, mode):
+        self.circuit.prepare_mode_displaced_squeezed(r_d, phi_d, r_s, phi_s, self._remap_modes(mode))
+
+    def prepare_thermal_state(self, nbar, mode):
+        self.circuit.prepare_mode_thermal(nbar, self._remap_modes(mode))
+
+    def prepare_fock_state(self, n, mode):
+        self.circuit.prepare_mode_fock(n, self._remap_modes(mode))
+
+    def prepare_ket_state(self, state, modes):
+        self.circuit.prepare_multimode(np.asarray(state), self._remap_modes(modes))
+
+    def prepare_dm_state(self, state, modes):
+        self.circuit.prepare_multimode(np.asarray(state), self._remap_modes(modes))
+
+    # ----------------------------------------------------------------- gates
+    def rotation(self, phi, mode):
+        self.circuit.phase_shift(phi, self._remap_modes(mode))
+
+    def displacement(self, r, phi, mode):
+        self.circuit.displacement(r, phi, self._remap_modes(mode))
+
+    def squeeze(self, r, phi, mode):
+        self.circuit.squeeze(r, phi, self._remap_modes(mode))
+
+    def two_mode_squeeze(self, r, phi, mode1, mode2):
+        self.circuit.two_mode_squeeze(r, phi, self._remap_modes(mode1), self._remap_modes(mode2))
+
+    def beamsplitter(self, theta, phi, mode1, mode2):
+        self.circuit.beamsplitter(theta, phi, self._remap_modes(mode1), self._remap_modes(mode2))
+
+    def mzgate(self, phi_in, phi_ex, mode1, mode2):
+        self.circuit.mzgate(phi_in, phi_ex, self._remap_modes(mode1), self._remap_modes(mode2))
+
+    def kerr_interaction(self, kappa, mode):
+        self.circuit.kerr_interaction(kappa, self._remap_modes(mode))
+
+    def cross_kerr_interaction(self, kappa, mode1, mode2):
+        self.circuit.cross_kerr_interaction(kappa, self._remap_modes(mode1), self._remap_modes(mode2))
+
+    def cubic_phase(self, gamma, mode):
+        self.circuit.cubic_phase_shift(gamma, self._remap_modes(mode))
+
+    def loss(self, T, mode):
+        self.circuit.loss(T, self._remap_modes(mode))
+
+    # ----------------------------------------------------------------- measurement
+    def measure_fock(self, modes, shots=1, select=None, **kwargs):
+        if shots != 1:
+            raise NotImplementedError(
+                "fock_gb300 backend currently does not support shots != 1 for Fock measurement")
+        return self.circuit.measure_fock(self._remap_modes(modes), select=select)
+
+    def measure_homodyne(self, phi, mode, shots=1, select=None, **kwargs):
+        raise NotImplementedError("fock_gb300 backend does not implement homodyne measurement yet")
+
+    def is_vacuum(self, tol=0.0, **kwargs):
+        return self.circuit.is_vacuum(tol)
+
+    # ----------------------------------------------------------------- state
+    def state(self, modes=None, **kwargs):
+        """Current state; ``modes`` selects a reduced (mixed) state
+        (reference fockbackend/backend.py:209-264)."""
+        s, pure = self.circuit.get_state()
+        num = self.circuit._num_modes
+        cutoff = self.circuit._trunc
+        if modes is None:
+            names = ["q[{}]".format(i) for i in self.get_modes()]
+            return FockStateGB300(s, num, pure, cutoff, names)
+        if isinstance(modes, int):
+            modes = [modes]
+        if len(modes) != len(set(modes)):
+            raise ValueError("The specified modes cannot be duplicated.")
+        if len(modes) > num:
+            raise ValueError("The number of specified modes cannot be larger than the number of subsystems.")
+        full = FockStateGB300(s, num, pure, cutoff)
+        srt = sorted(modes)
+        red = full.reduced_dm(srt) if srt != list(range(num)) else full.dm()
+        red = np.asarray(red).reshape([cutoff] * (2 * len(modes)))
+        if modes != srt:
+            perm = np.argsort(modes)
+            idx = [2 * x + i for x in perm for i in (0, 1)]
+            red = np.transpose(red, np.argsort(idx))
+        names = ["q[{}]".format(i) for i in np.array(self.get_modes())[modes]]
+        t = torch.as_tensor(np.ascontiguousarray(red), device=s.device).to(s.dtype)
+        return FockStateGB300(t, len(modes), False, cutoff, names)
+
+
+_SF_CLASS = None
+
+
+def sf_backend():
+    """A ``fock_gb300`` backend instance that is also a ``BaseFock`` of the
+    installed Strawberry Fields, for ``sf.Engine(sf_backend(), ...)``."""
+    global _SF_CLASS
+    if _SF_CLASS is None:
+        from strawberryfields.backends.base import BaseFock  # pylint: disable=import-outside-toplevel
+
+        _SF_CLASS = type("FockGB300Backend", (FockGB300Backend, BaseFock), {})
+    return _SF_CLASS()
+
+
+def register():
+    """Make ``sf.Engine("fock_gb300")`` resolve to this backend."""
+    from strawberryfields import backends  # pylint: disable=import-outside-toplevel
+
+    sf_backend()
+    backends.local_backends[FockGB300Backend.short_name] = _SF_CLASS
+    return _SF_CLASS

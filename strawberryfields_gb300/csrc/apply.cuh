@@ -1,0 +1,100 @@
+// Strided views of a state tensor for one- and two-axis gates, and the launch
+// interface of the apply / adjoint kernels.
+#pragma once
+#include "gates.cuh"
+
+// A gate on axes (ax1 < ax2) of a C-order [D]^naxes tensor sees the state as
+// [A][D][B][D][C] (two axes) or [A][D][C] (one axis; B = 1, s2 = 0).
+// Column j = (a, b, c), c fastest; element (a, i, b, k, c) sits at
+// base(j) + i*s1 + k*s2 with base(j) = a*D*s1 + b*D*s2 + c.
+struct AxisView {
+  int64_t A, B, C;
+  int64_t s1, s2;
+  int64_t ncols;
+};
+
+AxisView make_view1(int naxes, int D, int ax);
+AxisView make_view2(int naxes, int D, int ax1, int ax2);
+
+__device__ __forceinline__ int64_t col_base(const AxisView& v, int64_t j, int D) {
+  int64_t c = j % v.C;
+  int64_t t = j / v.C;
+  int64_t b = t % v.B;
+  int64_t a = t / v.B;
+  return a * (v.s1 * D) + b * (v.s2 * D) + c;
+}
+
+// matrix staging flags
+#define MF_CONJ 1     // use conj(M)            (bra side of a mixed state)
+#define MF_ADJOINT 2  // use M^dagger           (adjoint sweep)
+#define MF_SWAP 4     // view axes are (mode2, mode1) of the stored two-mode matrix
+
+// geometry of block b of a view: s entries, offsets base + boff + u*step
+struct BlockGeom {
+  int s;
+  int64_t boff, step;
+  int64_t moff;   // offset of the stored block in the matrix
+  int rev;        // stored position = s-1-u (swapped SUM blocks)
+};
+
+__device__ __forceinline__ BlockGeom block_geom(const AxisView& v, int D, int layout, int b, int swap) {
+  BlockGeom g;
+  if (layout == LAYOUT_DENSE) {
+    g.s = D; g.boff = 0; g.step = v.s1; g.moff = 0; g.rev = 0;
+    return g;
+  }
+  g.s = blk_size(D, b);
+  if (layout == LAYOUT_SUM) {
+    int lo = blk_lo(D, 1, b);
+    g.boff = (int64_t)lo * v.s1 + (int64_t)(b - lo) * v.s2;
+    g.step = v.s1 - v.s2;
+    g.moff = blk_offset(D, b);
+    g.rev = swap;
+  } else {
+    int delta = b - (D - 1);
+    int lo = delta > 0 ? delta : 0;
+    g.boff = (int64_t)lo * v.s1 + (int64_t)(lo - delta) * v.s2;
+    g.step = v.s1 + v.s2;
+    int bs = swap ? (2 * D - 2 - b) : b;
+    g.moff = blk_offset(D, bs);
+    g.rev = 0;
+  }
+  return g;
+}
+
+// Stage the s x s block for this CTA into shared memory in the state precision,
+// as the matrix that maps the view's input positions to its output positions.
+template <typename CT>
+__device__ __forceinline__ void stage_block(CT* Ms, const double2* mat, const BlockGeom& g, int mflags) {
+  const int s = g.s;
+  for (int e = threadIdx.x; e < s * s; e += blockDim.x) {
+    int w = e / s, u = e - w * s;  // view output w, view input u
+    int a = w, c = u;
+    if (mflags & MF_ADJOINT) { a = u; c = w; }  // (M^dag)[w][u] = conj(M[u][w])
+    if (g.rev) { a = s - 1 - a; c = s - 1 - c; }
+    double2 m = mat[g.moff + (int64_t)a * s + c];
+    int cj = ((mflags & MF_ADJOINT) ? 1 : 0) ^ ((mflags & MF_CONJ) ? 1 : 0);
+    if (cj) m.y = -m.y;
+    Ms[e] = to_c(m, (CT*)nullptr);
+  }
+}
+
+// Apply a built matrix (FP64 in `mat`, layout LAYOUT_*) on a view: out = M in.
+int launch_apply(int dtype, const void* in, void* out, const AxisView& v, int D, int layout,
+                 const double2* mat, int mflags, cudaStream_t st);
+
+// Adjoint step of one op: lam_in = M^dagger lam_out (skipped when lam_in is
+// null) and the per-CTA partial sums of
+// C[u][v] = sum over columns conj(lam_out[u]) psi_in[v] (stored-matrix
+// orientation, FP64), written to cpart[gx][entries] with gx =
+// adjoint_grid_x(...).  launch_reduce_partials sums them in a fixed order.
+int launch_adjoint_partials(int dtype, const void* psi_in, const void* lam_out, void* lam_in,
+                            const AxisView& v, int D, int layout, const double2* mat, int mflags,
+                            double2* cpart, int gx, cudaStream_t st);
+int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* cout, cudaStream_t st);
+int64_t adjoint_scratch_entries(int dtype, const AxisView& v, int D, int layout);
+int adjoint_grid_x(int dtype, const AxisView& v, int D, int layout);
+
+// single matrix build with inline parameters (gates.cu)
+int build_single(int gate, int layout, int D, double p0, double p1, const PhaseTerm* terms,
+                 int nterm, double2* M, double2* dM, double2* scratch, cudaStream_t st);

@@ -1,0 +1,566 @@
+// Compiled circuits: gate-list fusion, forward sweep and adjoint sweep.
+//
+// fock_plan_create compiles a gate list on the host.  Rotation and Kerr gates
+// (diagonal in the Fock basis) never get their own pass over the state: they
+// become phase terms of the next non-diagonal gate on the same mode (input
+// side), or of the last one (output side) when no later gate touches the
+// mode; cross-Kerr becomes a phase term of a two-mode gate on the same pair
+// or, failing that, its own identity op.  Each remaining op reads and writes
+// the state once.  The reference applies every gate as its own pass
+// (LocalEngine._run_program, strawberryfields/engine.py:422-471, calling
+// Circuit.apply_gate_BLAS / apply_twomode_gate per gate).
+//
+// Device tables (build jobs, phase terms, gradient contributions) live at the
+// head of the caller's workspace and are copied there from pinned host memory
+// on every call, so a captured CUDA graph replays them.
+#include "apply.cuh"
+
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+namespace {
+
+struct PlanOp {
+  int layout = 0;
+  int gate = GATE_IDENTITY;
+  int mode1 = -1, mode2 = -1;
+  int pidx = -1;
+  int n_fused = 0;
+  std::vector<PhaseTerm> terms;
+  std::vector<GradContrib> contribs;  // .op filled at finalize
+  // derived
+  AxisView view;
+  int swap = 0;
+  int64_t m_off = 0, dm_off = -1, scratch_off = -1, c_off = 0, cpart_off = 0;
+  int gx = 1;
+  int64_t nent = 0;
+};
+
+struct RedOp {
+  int64_t c_off, cpart_off, nent;
+  int gx, pad_;
+};
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+struct fock_plan {
+  int N = 0, D = 0, pure = 1, dtype = 0, n_params = 0, n_gates = 0;
+  std::vector<PlanOp> ops;
+  // table image (pinned host memory) and its sections
+  unsigned char* host = nullptr;
+  size_t tables_bytes = 0;
+  size_t o_jobs = 0, o_terms = 0, o_gops = 0, o_contrib = 0, o_pstart = 0, o_plist = 0, o_red = 0;
+  int n_terms = 0, n_contrib = 0;
+  // workspace sections
+  size_t o_arena = 0, o_carena = 0, o_cpart = 0, ws_bytes = 0;
+  int64_t arena_entries = 0, carena_entries = 0, cpart_entries = 0;
+  int64_t state_elems = 0;
+  int64_t flops_fwd = 0;
+  // optional per-op timing
+  int timing = 0;
+  std::vector<cudaEvent_t> ev_fwd, ev_bwd;
+  int fwd_recorded = 0, bwd_recorded = 0;
+};
+
+static int ensure_events(std::vector<cudaEvent_t>& ev, size_t n) {
+  while (ev.size() < n) {
+    cudaEvent_t e;
+    FOCK_CUDA_TRY(cudaEventCreate(&e));
+    ev.push_back(e);
+  }
+  return FOCK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched reduction of all ops' partial C sums
+// ---------------------------------------------------------------------------
+__global__ void reduce_all_kernel(const RedOp* __restrict__ ops, int n_ops, int64_t total,
+                                  const double2* __restrict__ cpart, double2* __restrict__ carena) {
+  const int lane = threadIdx.x & 31;
+  const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (e >= total) return;
+  int lo = 0, hi = n_ops - 1;
+  while (lo < hi) {  // last op with c_off <= e
+    int mid = (lo + hi + 1) >> 1;
+    if (ops[mid].c_off <= e) lo = mid;
+    else hi = mid - 1;
+  }
+  const RedOp R = ops[lo];
+  const int64_t le = e - R.c_off;
+  double2 a = make_double2(0.0, 0.0);
+  for (int x = lane; x < R.gx; x += 32) {
+    double2 p = cpart[R.cpart_off + (int64_t)x * R.nent + le];
+    a.x += p.x;
+    a.y += p.y;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    a.x += __shfl_xor_sync(0xffffffffu, a.x, off);
+    a.y += __shfl_xor_sync(0xffffffffu, a.y, off);
+  }
+  if (lane == 0) carena[e] = a;
+}
+
+// ---------------------------------------------------------------------------
+// compile
+// ---------------------------------------------------------------------------
+static int is_diag1(int k) { return k == FOCK_ROTATION || k == FOCK_KERR; }
+static int is_two(int k) {
+  return k == FOCK_BEAMSPLITTER || k == FOCK_MZGATE || k == FOCK_CROSS_KERR || k == FOCK_TWO_MODE_SQUEEZE;
+}
+
+// add a phase term (with its gradient contribution) to op
+static void add_term(PlanOp& op, int fn, int side, int pidx) {
+  op.terms.push_back(PhaseTerm{fn, side, pidx, 0, 0.0});
+  GradContrib g;
+  g.op = -1;
+  g.type = side ? GC_W_OUT : GC_W_IN;
+  g.fn = fn;
+  g.pidx = pidx;
+  g.scale = 1.0;
+  op.contribs.push_back(g);
+  op.n_fused++;
+}
+
+static void add_contrib(PlanOp& op, int type, int fn, int pidx, double scale) {
+  GradContrib g;
+  g.op = -1;
+  g.type = type;
+  g.fn = fn;
+  g.pidx = pidx;
+  g.scale = scale;
+  op.contribs.push_back(g);
+}
+
+struct Pending {
+  int fn;     // FN_A (rotation) or FN_A2 (Kerr) relative to the mode
+  int pidx;
+};
+struct PendingCK {
+  int a, b, pidx;
+};
+
+// move pending single-mode terms of `mode` into op as input-side terms
+static void absorb_pending(PlanOp& op, int mode, std::vector<std::vector<Pending>>& pend) {
+  const int slot_b = (op.layout != LAYOUT_DENSE && op.mode2 == mode);
+  for (const Pending& p : pend[mode]) {
+    int fn = p.fn;
+    if (slot_b) fn = (fn == FN_A) ? FN_B : FN_B2;
+    add_term(op, fn, 0, p.pidx);
+  }
+  pend[mode].clear();
+}
+
+extern "C" int fock_plan_create(int num_modes, int cutoff, int pure, int dtype, const fock_gate* gates,
+                                int n_gates, int n_params, fock_plan** out) {
+  if (!out) return fock_set_error(FOCK_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  if (dtype != FOCK_C64 && dtype != FOCK_C128) return fock_set_error(FOCK_ERR_INVALID, "bad dtype");
+  if (cutoff < 1 || cutoff > FOCK_MAX_CUTOFF) return fock_set_error(FOCK_ERR_INVALID, "bad cutoff %d", cutoff);
+  if (num_modes < 1 || num_modes > FOCK_MAX_AXES / 2) return fock_set_error(FOCK_ERR_INVALID, "bad number of modes");
+  if (!pure) return fock_set_error(FOCK_ERR_UNSUPPORTED, "compiled circuits support pure states");
+  if (n_gates < 0 || (n_gates > 0 && !gates)) return fock_set_error(FOCK_ERR_INVALID, "bad gate list");
+  if (n_params < 0) return fock_set_error(FOCK_ERR_INVALID, "bad parameter count");
+  if (num_modes * log2((double)cutoff) > 60.0) return fock_set_error(FOCK_ERR_INVALID, "state too large");
+
+  fock_plan* P = new fock_plan();
+  P->N = num_modes; P->D = cutoff; P->pure = pure; P->dtype = dtype; P->n_params = n_params;
+  P->n_gates = n_gates;
+  const int N = num_modes, D = cutoff;
+
+  std::vector<std::vector<Pending>> pend(N);
+  std::vector<PendingCK> pck;
+  std::vector<int> last_op(N, -1);
+
+  auto fail = [&](int code, const char* msg, int g) {
+    delete P;
+    return fock_set_error(code, "gate %d: %s", g, msg);
+  };
+
+  auto flush_ck = [&](size_t idx) {
+    // standalone identity op on the pair carrying the cross-Kerr phase
+    PendingCK c = pck[idx];
+    PlanOp op;
+    op.layout = LAYOUT_SUM;
+    op.gate = GATE_IDENTITY;
+    op.mode1 = c.a;
+    op.mode2 = c.b;
+    absorb_pending(op, c.a, pend);
+    absorb_pending(op, c.b, pend);
+    add_term(op, FN_AB, 0, c.pidx);
+    P->ops.push_back(op);
+    last_op[c.a] = last_op[c.b] = (int)P->ops.size() - 1;
+  };
+
+  for (int g = 0; g < n_gates; ++g) {
+    const fock_gate& G = gates[g];
+    const int two = is_two(G.kind);
+    if (G.mode1 < 0 || G.mode1 >= N) return fail(FOCK_ERR_INVALID, "invalid mode", g);
+    if (two && (G.mode2 < 0 || G.mode2 >= N || G.mode2 == G.mode1)) return fail(FOCK_ERR_INVALID, "invalid second mode", g);
+    const int np = (G.kind == FOCK_ROTATION || G.kind == FOCK_KERR || G.kind == FOCK_CROSS_KERR || G.kind == FOCK_LOSS) ? 1 : 2;
+    if (G.pidx < 0 || G.pidx + np > n_params) return fail(FOCK_ERR_INVALID, "parameter index out of range", g);
+    if (G.kind == FOCK_LOSS) return fail(FOCK_ERR_UNSUPPORTED, "loss channel in a pure-state circuit", g);
+    if (is_diag1(G.kind)) {
+      pend[G.mode1].push_back(Pending{G.kind == FOCK_ROTATION ? FN_A : FN_A2, G.pidx});
+      continue;
+    }
+    if (G.kind == FOCK_CROSS_KERR) {
+      pck.push_back(PendingCK{G.mode1, G.mode2, G.pidx});
+      continue;
+    }
+    const int layout = gate_layout(G.kind);
+    if (!layout) return fail(FOCK_ERR_INVALID, "unknown gate kind", g);
+    // cross-Kerr pending on a mode this gate touches must be applied first,
+    // unless this gate acts on exactly that pair (then it becomes a phase term)
+    PlanOp op;
+    op.layout = layout;
+    op.gate = G.kind;
+    op.mode1 = G.mode1;
+    op.mode2 = two ? G.mode2 : -1;
+    op.pidx = G.pidx;
+    op.n_fused = 1;
+    std::vector<PendingCK> keep;
+    std::vector<PendingCK> fuse_here;
+    for (size_t i = 0; i < pck.size(); ++i) {
+      const PendingCK& c = pck[i];
+      const bool touches = c.a == G.mode1 || c.b == G.mode1 || (two && (c.a == G.mode2 || c.b == G.mode2));
+      if (!touches) { keep.push_back(c); continue; }
+      const bool same_pair = two && ((c.a == G.mode1 && c.b == G.mode2) || (c.a == G.mode2 && c.b == G.mode1));
+      if (same_pair) fuse_here.push_back(c);
+      else {
+        pck[i] = c;
+        flush_ck(i);
+      }
+    }
+    pck = keep;
+    absorb_pending(op, G.mode1, pend);
+    if (two) absorb_pending(op, G.mode2, pend);
+    for (const PendingCK& c : fuse_here) add_term(op, FN_AB, 0, c.pidx);
+    switch (G.kind) {
+      case FOCK_DISPLACEMENT:
+        add_contrib(op, GC_DM, 0, G.pidx, 1.0);
+        add_contrib(op, GC_W_DIFF, FN_A, G.pidx + 1, 1.0);
+        break;
+      case FOCK_SQUEEZE:
+        add_contrib(op, GC_DM, 0, G.pidx, 1.0);
+        add_contrib(op, GC_W_DIFF, FN_A, G.pidx + 1, 0.5);
+        break;
+      case FOCK_BEAMSPLITTER:
+        add_contrib(op, GC_DM, 0, G.pidx, 1.0);
+        add_contrib(op, GC_W_DIFF, FN_B, G.pidx + 1, 1.0);
+        break;
+      case FOCK_TWO_MODE_SQUEEZE:
+        add_contrib(op, GC_DM, 0, G.pidx, 1.0);
+        add_contrib(op, GC_W_DIFF, FN_A, G.pidx + 1, 1.0);
+        break;
+      case FOCK_MZGATE:
+        // MZ(phi_in, phi_ex): R(phi_ex) on mode1 first, carried as a phase term
+        add_contrib(op, GC_DM, 0, G.pidx, 1.0);
+        add_term(op, FN_A, 0, G.pidx + 1);
+        op.n_fused--;  // part of the gate itself
+        break;
+      default:
+        break;
+    }
+    P->ops.push_back(op);
+    last_op[G.mode1] = (int)P->ops.size() - 1;
+    if (two) last_op[G.mode2] = (int)P->ops.size() - 1;
+  }
+  // leftovers: cross-Kerr as identity ops, then single-mode phases as output
+  // terms of the last op on the mode (or an identity op)
+  for (size_t i = 0; i < pck.size(); ++i) flush_ck(i);
+  pck.clear();
+  for (int m = 0; m < N; ++m) {
+    if (pend[m].empty()) continue;
+    if (last_op[m] < 0) {
+      PlanOp op;
+      op.layout = LAYOUT_DENSE;
+      op.gate = GATE_IDENTITY;
+      op.mode1 = m;
+      absorb_pending(op, m, pend);
+      P->ops.push_back(op);
+      last_op[m] = (int)P->ops.size() - 1;
+      continue;
+    }
+    PlanOp& op = P->ops[last_op[m]];
+    const int slot_b = (op.layout != LAYOUT_DENSE && op.mode2 == m);
+    for (const Pending& p : pend[m]) {
+      int fn = p.fn;
+      if (slot_b) fn = (fn == FN_A) ? FN_B : FN_B2;
+      add_term(op, fn, 1, p.pidx);
+    }
+    pend[m].clear();
+  }
+
+  // layout of arena / C arena / partials, and tables
+  int64_t elems = 1;
+  for (int k = 0; k < N; ++k) elems *= D;
+  P->state_elems = elems;
+  int64_t arena = 0, carena = 0, cpart = 0;
+  int n_terms = 0, n_contrib = 0;
+  for (size_t k = 0; k < P->ops.size(); ++k) {
+    PlanOp& op = P->ops[k];
+    op.nent = layout_entries(op.layout, D);
+    op.m_off = arena;
+    arena += op.nent;
+    const bool has_dm = op.gate != GATE_IDENTITY;
+    if (has_dm) { op.dm_off = arena; arena += op.nent; }
+    const int64_t ns = build_scratch_entries(op.gate, D);
+    if (ns > 0) { op.scratch_off = arena; arena += ns; }
+    if (op.layout == LAYOUT_DENSE) op.view = make_view1(N, D, op.mode1);
+    else {
+      int a = op.mode1, b = op.mode2;
+      op.swap = a > b;
+      op.view = make_view2(N, D, std::min(a, b), std::max(a, b));
+    }
+    op.gx = adjoint_grid_x(dtype, op.view, D, op.layout);
+    op.c_off = carena;
+    carena += op.nent;
+    op.cpart_off = cpart;
+    cpart += (int64_t)op.gx * op.nent;
+    n_terms += (int)op.terms.size();
+    n_contrib += (int)op.contribs.size();
+    // flops: 8 real flops per complex multiply-add
+    int64_t macs_per_col = op.layout == LAYOUT_DENSE ? (int64_t)D * D : blk_total(D);
+    P->flops_fwd += 8 * macs_per_col * op.view.ncols;
+  }
+  P->arena_entries = arena;
+  P->carena_entries = carena;
+  P->cpart_entries = cpart;
+  P->n_terms = n_terms;
+  P->n_contrib = n_contrib;
+  const int n_ops = (int)P->ops.size();
+  size_t o = 0;
+  P->o_jobs = o; o = align256(o + sizeof(BuildJob) * std::max(n_ops, 1));
+  P->o_terms = o; o = align256(o + sizeof(PhaseTerm) * std::max(n_terms, 1));
+  P->o_gops = o; o = align256(o + sizeof(GradOp) * std::max(n_ops, 1));
+  P->o_contrib = o; o = align256(o + sizeof(GradContrib) * std::max(n_contrib, 1));
+  P->o_pstart = o; o = align256(o + sizeof(int) * (n_params + 1));
+  P->o_plist = o; o = align256(o + sizeof(int) * std::max(n_contrib, 1));
+  P->o_red = o; o = align256(o + sizeof(RedOp) * std::max(n_ops, 1));
+  P->tables_bytes = o;
+  P->o_arena = o; o = align256(o + sizeof(double2) * arena);
+  P->o_carena = o; o = align256(o + sizeof(double2) * std::max<int64_t>(carena, 1));
+  P->o_cpart = o; o = align256(o + sizeof(double2) * std::max<int64_t>(cpart, 1));
+  P->ws_bytes = o;
+
+  if (cudaHostAlloc((void**)&P->host, P->tables_bytes, cudaHostAllocDefault) != cudaSuccess) {
+    // fall back to pageable memory (copies are then synchronous)
+    cudaGetLastError();
+    P->host = (unsigned char*)malloc(P->tables_bytes);
+    if (!P->host) { delete P; return fock_set_error(FOCK_ERR_INVALID, "out of host memory"); }
+  }
+  memset(P->host, 0, P->tables_bytes);
+  BuildJob* jobs = (BuildJob*)(P->host + P->o_jobs);
+  PhaseTerm* terms = (PhaseTerm*)(P->host + P->o_terms);
+  GradOp* gops = (GradOp*)(P->host + P->o_gops);
+  GradContrib* contrib = (GradContrib*)(P->host + P->o_contrib);
+  int* pstart = (int*)(P->host + P->o_pstart);
+  int* plist = (int*)(P->host + P->o_plist);
+  RedOp* red = (RedOp*)(P->host + P->o_red);
+  int t = 0, c = 0;
+  std::vector<std::vector<int>> by_param(n_params);
+  for (int k = 0; k < n_ops; ++k) {
+    PlanOp& op = P->ops[k];
+    BuildJob& J = jobs[k];
+    J.gate = op.gate;
+    J.layout = op.layout;
+    J.D = D;
+    J.pidx = op.pidx;
+    J.v0 = J.v1 = 0.0;
+    J.term0 = t;
+    J.nterm = (int)op.terms.size();
+    J.m_off = op.m_off;
+    J.dm_off = op.dm_off;
+    J.scratch_off = op.scratch_off;
+    for (const PhaseTerm& pt : op.terms) terms[t++] = pt;
+    GradOp& go = gops[k];
+    go.layout = op.layout;
+    go.D = D;
+    go.m_off = op.m_off;
+    go.dm_off = op.dm_off;
+    go.c_off = op.c_off;
+    go.nent = (int)op.nent;
+    for (GradContrib gc : op.contribs) {
+      gc.op = k;
+      contrib[c] = gc;
+      by_param[gc.pidx].push_back(c);
+      ++c;
+    }
+    red[k].c_off = op.c_off;
+    red[k].cpart_off = op.cpart_off;
+    red[k].nent = op.nent;
+    red[k].gx = op.gx;
+  }
+  int q = 0;
+  for (int p = 0; p < n_params; ++p) {
+    pstart[p] = q;
+    for (int ci : by_param[p]) plist[q++] = ci;
+  }
+  pstart[n_params] = q;
+  *out = P;
+  return FOCK_OK;
+}
+
+extern "C" void fock_plan_destroy(fock_plan* P) {
+  if (!P) return;
+  for (cudaEvent_t e : P->ev_fwd) cudaEventDestroy(e);
+  for (cudaEvent_t e : P->ev_bwd) cudaEventDestroy(e);
+  if (P->host) {
+    if (cudaFreeHost(P->host) != cudaSuccess) {
+      cudaGetLastError();
+      free(P->host);
+    }
+  }
+  delete P;
+}
+
+extern "C" int fock_plan_get_info(const fock_plan* P, fock_plan_info* info) {
+  if (!P || !info) return fock_set_error(FOCK_ERR_INVALID, "null argument");
+  info->n_ops = (int32_t)P->ops.size();
+  info->n_gates = P->n_gates;
+  info->state_elems = P->state_elems;
+  info->state_bytes = P->state_elems * (P->dtype == FOCK_C64 ? 8 : 16);
+  info->workspace_bytes = (int64_t)P->ws_bytes;
+  info->flops_fwd = P->flops_fwd;
+  info->bytes_fwd = 2 * info->state_bytes * (int64_t)P->ops.size();
+  return FOCK_OK;
+}
+
+extern "C" int fock_plan_op(const fock_plan* P, int k, int* kind, int* mode1, int* mode2, int* n_fused) {
+  if (!P || k < 0 || k >= (int)P->ops.size()) return fock_set_error(FOCK_ERR_INVALID, "bad op index");
+  const PlanOp& op = P->ops[k];
+  if (kind) *kind = op.layout;
+  if (mode1) *mode1 = op.mode1;
+  if (mode2) *mode2 = op.mode2;
+  if (n_fused) *n_fused = op.n_fused;
+  return FOCK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// execution
+// ---------------------------------------------------------------------------
+static int upload_and_build(fock_plan* P, const double* params, unsigned char* ws, int with_deriv,
+                            cudaStream_t st) {
+  FOCK_CUDA_TRY(cudaMemcpyAsync(ws, P->host, P->tables_bytes, cudaMemcpyHostToDevice, st));
+  const int n_ops = (int)P->ops.size();
+  if (!with_deriv) {
+    // forward only needs M: a job table with dm_off = -1 would need a second
+    // table; building dM as well costs one extra matrix write per op and keeps
+    // one table
+  }
+  return launch_build_jobs((const BuildJob*)(ws + P->o_jobs), n_ops, (const PhaseTerm*)(ws + P->o_terms),
+                           params, (double2*)(ws + P->o_arena), st);
+}
+
+extern "C" int fock_plan_forward(fock_plan* P, const double* params, const void* state_in, void* states,
+                                 int store_all, void* workspace, void* stream) {
+  if (!P) return fock_set_error(FOCK_ERR_INVALID, "null plan");
+  if (!state_in || !states || !workspace) return fock_set_error(FOCK_ERR_INVALID, "null buffer");
+  if (P->n_params > 0 && !params) return fock_set_error(FOCK_ERR_INVALID, "null parameter array");
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned char* ws = (unsigned char*)workspace;
+  int rc = upload_and_build(P, params, ws, 0, st);
+  if (rc) return rc;
+  const int esz = P->dtype == FOCK_C64 ? 8 : 16;
+  const int64_t sb = P->state_elems * esz;
+  const double2* arena = (const double2*)(ws + P->o_arena);
+  const void* cur = state_in;
+  const int n_ops = (int)P->ops.size();
+  if (P->timing) {
+    if ((rc = ensure_events(P->ev_fwd, n_ops + 1))) return rc;
+    P->fwd_recorded = 0;
+  }
+  for (int k = 0; k < n_ops; ++k) {
+    const PlanOp& op = P->ops[k];
+    void* dst = (char*)states + (store_all ? (int64_t)k : (int64_t)(k & 1)) * sb;
+    if (P->timing) FOCK_CUDA_TRY(cudaEventRecord(P->ev_fwd[k], st));
+    rc = launch_apply(P->dtype, cur, dst, op.view, P->D, op.layout, arena + op.m_off, op.swap ? MF_SWAP : 0, st);
+    if (rc) return rc;
+    cur = dst;
+  }
+  if (P->timing) {
+    FOCK_CUDA_TRY(cudaEventRecord(P->ev_fwd[n_ops], st));
+    P->fwd_recorded = 1;
+  }
+  return FOCK_OK;
+}
+
+extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void* state_in,
+                                  const void* states, void* grad_state, void* grad_tmp, double* grad_params,
+                                  void* workspace, void* stream) {
+  if (!P) return fock_set_error(FOCK_ERR_INVALID, "null plan");
+  if (!state_in || !states || !grad_state || !grad_tmp || !workspace)
+    return fock_set_error(FOCK_ERR_INVALID, "null buffer");
+  if (P->n_params > 0 && (!params || !grad_params)) return fock_set_error(FOCK_ERR_INVALID, "null parameter array");
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned char* ws = (unsigned char*)workspace;
+  int rc = upload_and_build(P, params, ws, 1, st);
+  if (rc) return rc;
+  const int esz = P->dtype == FOCK_C64 ? 8 : 16;
+  const int64_t sb = P->state_elems * esz;
+  const double2* arena = (const double2*)(ws + P->o_arena);
+  double2* cpart = (double2*)(ws + P->o_cpart);
+  const int n_ops = (int)P->ops.size();
+  void* lam = grad_state;
+  void* other = grad_tmp;
+  if (P->timing) {
+    if ((rc = ensure_events(P->ev_bwd, n_ops + 1))) return rc;
+    P->bwd_recorded = 0;
+  }
+  for (int k = n_ops - 1; k >= 0; --k) {
+    const PlanOp& op = P->ops[k];
+    const void* psi_in = k == 0 ? state_in : (const char*)states + (int64_t)(k - 1) * sb;
+    if (P->timing) FOCK_CUDA_TRY(cudaEventRecord(P->ev_bwd[k + 1], st));
+    rc = launch_adjoint_partials(P->dtype, psi_in, lam, other, op.view, P->D, op.layout, arena + op.m_off,
+                                 op.swap ? MF_SWAP : 0, cpart + op.cpart_off, op.gx, st);
+    if (rc) return rc;
+    void* t = lam;
+    lam = other;
+    other = t;
+  }
+  if (P->timing) {
+    FOCK_CUDA_TRY(cudaEventRecord(P->ev_bwd[0], st));
+    P->bwd_recorded = 1;
+  }
+  if (lam != grad_state) FOCK_CUDA_TRY(cudaMemcpyAsync(grad_state, lam, sb, cudaMemcpyDeviceToDevice, st));
+  if (n_ops > 0) {
+    const int64_t threads = P->carena_entries * 32;
+    reduce_all_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+        (const RedOp*)(ws + P->o_red), n_ops, P->carena_entries, cpart, (double2*)(ws + P->o_carena));
+    FOCK_LAUNCH_CHECK("reduce_all_kernel");
+  }
+  if (P->n_params > 0) {
+    rc = launch_param_grads((const GradOp*)(ws + P->o_gops), (const GradContrib*)(ws + P->o_contrib),
+                            (const int*)(ws + P->o_pstart), (const int*)(ws + P->o_plist), P->n_params,
+                            (const PhaseTerm*)(ws + P->o_terms), arena, (const double2*)(ws + P->o_carena),
+                            grad_params, st);
+    if (rc) return rc;
+  }
+  return FOCK_OK;
+}
+
+extern "C" int fock_plan_enable_timing(fock_plan* P, int enable) {
+  if (!P) return fock_set_error(FOCK_ERR_INVALID, "null plan");
+  P->timing = enable ? 1 : 0;
+  return FOCK_OK;
+}
+
+extern "C" int fock_plan_op_times(fock_plan* P, float* fwd_ms, float* bwd_ms) {
+  if (!P) return fock_set_error(FOCK_ERR_INVALID, "null plan");
+  const int n = (int)P->ops.size();
+  if (fwd_ms) {
+    if (!P->fwd_recorded) return fock_set_error(FOCK_ERR_INVALID, "no timed forward sweep recorded");
+    for (int k = 0; k < n; ++k) FOCK_CUDA_TRY(cudaEventElapsedTime(&fwd_ms[k], P->ev_fwd[k], P->ev_fwd[k + 1]));
+  }
+  if (bwd_ms) {
+    if (!P->bwd_recorded) return fock_set_error(FOCK_ERR_INVALID, "no timed backward sweep recorded");
+    // ev_bwd[k+1] was recorded before op k's adjoint, ev_bwd[k] after it
+    for (int k = 0; k < n; ++k) FOCK_CUDA_TRY(cudaEventElapsedTime(&bwd_ms[k], P->ev_bwd[k + 1], P->ev_bwd[k]));
+  }
+  return FOCK_OK;
+}

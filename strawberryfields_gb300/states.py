@@ -1,0 +1,263 @@
+"""State object returned by the GB300 backend: the counterpart of
+``BaseFockState`` (reference ``strawberryfields/backends/states.py:477-986``).
+
+Readouts run on the device: probabilities, per-mode photon-number marginals
+and single-mode reduced density matrices never form the full density matrix
+of a pure state (the reference's ``reduced_dm``/``mean_photon`` build it,
+states.py:613-663).  ``ket()``/``dm()`` copy to the host as numpy arrays, like
+the reference; ``ket_tensor()`` exposes the device tensor without a copy.
+"""
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+
+class FockStateGB300:
+    """Fock-basis state held on the GPU.
+
+    Args:
+        state_data (torch.Tensor): device state tensor (captured as is)
+        num_modes (int): number of modes
+        pure (bool): ket ([D]*n) or density matrix ([D]*2n, interleaved axes)
+        cutoff_dim (int): Fock cutoff D
+        mode_names (Sequence[str]): optional mode names
+        hbar (float): value of hbar for quadrature readouts
+    """
+
+    EQ_TOLERANCE = 1e-10
+
+    def __init__(self, state_data, num_modes, pure, cutoff_dim, mode_names=None, hbar=2.0):
+        # same argument order as BaseFockState (states.py:489); state_data is
+        # a CUDA tensor ([D]*n pure, [D]*2n mixed) or a host array
+        if not torch.is_tensor(state_data):
+            state_data = torch.as_tensor(np.asarray(state_data), device="cuda")
+        self._tensor = state_data
+        self._pure = bool(pure)
+        self._modes = num_modes
+        self._cutoff = cutoff_dim
+        self._hbar = hbar
+        self._basis = "fock"
+        self._dcode = L.C64 if state_data.dtype == torch.complex64 else L.C128
+        if state_data.dtype not in (torch.complex64, torch.complex128):
+            self._tensor = state_data.to(torch.complex128)
+            self._dcode = L.C128
+        if mode_names is None:
+            self._modemap = {i: "mode {}".format(i) for i in range(self._modes)}
+        else:
+            self._modemap = {i: "{}".format(j) for i, j in zip(range(self._modes), mode_names)}
+        self._str = "<FockState: num_modes={}, cutoff={}, pure={}, hbar={}>".format(
+            self._modes, self._cutoff, self._pure, self._hbar)
+
+    def __str__(self):
+        return self._str
+
+    __repr__ = __str__
+
+    # ----------------------------------------------------------------- basics
+    @property
+    def num_modes(self):
+        return self._modes
+
+    @property
+    def cutoff_dim(self):
+        return self._cutoff
+
+    @property
+    def is_pure(self):
+        return self._pure
+
+    @property
+    def hbar(self):
+        return self._hbar
+
+    @property
+    def mode_names(self):
+        return self._modemap
+
+    @property
+    def mode_indices(self):
+        return {v: k for k, v in self._modemap.items()}
+
+    @property
+    def data(self):
+        return self._tensor.cpu().numpy()
+
+    def ket_tensor(self):
+        """Device tensor of the ket (no copy); None for mixed states."""
+        return self._tensor if self._pure else None
+
+    def ket(self, **kwargs):
+        if self._pure:
+            return self._tensor.cpu().numpy()
+        return None
+
+    def dm(self, **kwargs):
+        if not self._pure:
+            return self._tensor.cpu().numpy()
+        D, n = self._cutoff, self._modes
+        dm = torch.empty([D] * (2 * n), dtype=self._tensor.dtype, device=self._tensor.device)
+        L.call("fock_mix", n, D, self._dcode, self._tensor.data_ptr(), dm.data_ptr(),
+               torch.cuda.current_stream(self._tensor.device).cuda_stream)
+        return dm.cpu().numpy()
+
+    # ----------------------------------------------------------------- readouts
+    def _probs_tensor(self):
+        D, n = self._cutoff, self._modes
+        out = torch.empty([D] * n, dtype=torch.float64, device=self._tensor.device)
+        L.call("fock_probs", n, D, int(self._pure), self._dcode, self._tensor.data_ptr(), out.data_ptr(),
+               torch.cuda.current_stream(self._tensor.device).cuda_stream)
+        return out
+
+    def all_fock_probs(self, **kwargs):
+        """Probabilities of all Fock basis states (states.py:580)."""
+        return self._probs_tensor().cpu().numpy()
+
+    def trace(self, **kwargs):
+        return float(self._probs_tensor().sum().item())
+
+    def fock_prob(self, n, **kwargs):
+        """Probability of one Fock basis state (states.py:644)."""
+        if len(n) != self._modes:
+            raise ValueError("List length should be equal to number of modes")
+        if max(n) >= self._cutoff:
+            raise ValueError("Can't get distribution beyond truncation level")
+        if self._pure:
+            v = self._tensor[tuple(n)].item()
+            return abs(v) ** 2
+        idx = tuple(n[i // 2] for i in range(len(n) * 2))
+        return float(self._tensor[idx].real.item())
+
+    def marginals(self):
+        """Photon-number distribution of every mode, numpy [n, D] (one device pass per mode)."""
+        D, n = self._cutoff, self._modes
+        out = torch.empty((n, D), dtype=torch.float64, device=self._tensor.device)
+        lib = L.load()
+        ws = torch.empty(lib.fock_marginals_workspace_bytes(n, D, int(self._pure), self._dcode),
+                         dtype=torch.uint8, device=self._tensor.device)
+        L.call("fock_marginals", n, D, int(self._pure), self._dcode, self._tensor.data_ptr(), out.data_ptr(),
+               ws.data_ptr(), torch.cuda.current_stream(self._tensor.device).cuda_stream)
+        return out.cpu().numpy()
+
+    def mean_photon(self, mode, **kwargs):
+        """(mean, variance) of the photon number of one mode (states.py:657)."""
+        p = self.marginals()[mode]
+        k = np.arange(self._cutoff)
+        mean = float(np.sum(k * p))
+        var = float(np.sum(k * k * p) - mean ** 2)
+        return mean, var
+
+    def _rdm1(self, mode):
+        D, n = self._cutoff, self._modes
+        out = torch.empty((D, D), dtype=torch.complex128, device=self._tensor.device)
+        lib = L.load()
+        ws = torch.empty(lib.fock_reduced_dm1_workspace_bytes(n, D, int(self._pure), self._dcode),
+                         dtype=torch.uint8, device=self._tensor.device)
+        L.call("fock_reduced_dm1", n, D, int(self._pure), self._dcode, mode, self._tensor.data_ptr(),
+               out.data_ptr(), ws.data_ptr(), torch.cuda.current_stream(self._tensor.device).cuda_stream)
+        return out.cpu().numpy()
+
+    def reduced_dm(self, modes, **kwargs):
+        """Reduced density matrix (states.py:613).  One mode: device
+        contraction; several modes: the kept modes' block of the density
+        matrix, interleaved axes like the reference."""
+        if isinstance(modes, int):
+            modes = [modes]
+        modes = list(modes)
+        if modes != sorted(modes):
+            raise ValueError("The specified modes cannot be duplicated.")
+        if len(modes) > self._modes:
+            raise ValueError("The number of specified modes cannot be larger than the number of subsystems.")
+        if modes == list(range(self._modes)):
+            return self.dm()
+        if len(modes) == 1:
+            return self._rdm1(modes[0])
+        return self._reduced_multi(modes)
+
+    def _reduced_multi(self, modes):
+        D, n = self._cutoff, self._modes
+        k = len(modes)
+        rest = [m for m in range(n) if m not in modes]
+        if self._pure:
+            psi = self._tensor.permute(modes + rest).reshape(D ** k, -1)
+            rho = (psi @ psi.conj().T).reshape([D] * (2 * k))
+            perm = []
+            for i in range(k):
+                perm += [i, k + i]
+            return rho.permute(perm).to(torch.complex128).cpu().numpy()
+        rho = self._tensor
+        # trace out the rest, last mode first so axis numbers stay valid
+        for m in sorted(rest, reverse=True):
+            rho = torch.diagonal(rho, dim1=2 * m, dim2=2 * m + 1).sum(-1)
+        return rho.to(torch.complex128).cpu().numpy()
+
+    # ----------------------------------------------------------------- fidelities
+    def fidelity(self, other_state, mode, **kwargs):
+        rho = self._rdm1(mode)
+        return float(np.dot(np.conj(other_state), np.dot(rho, other_state)).real)
+
+    def fidelity_vacuum(self, **kwargs):
+        if self._pure:
+            return abs(self._tensor.reshape(-1)[0].item()) ** 2
+        return float(self._tensor.reshape(-1)[0].real.item())
+
+    def fidelity_coherent(self, alpha_list, **kwargs):
+        if not hasattr(alpha_list, "__len__"):
+            alpha_list = [alpha_list]
+        if len(alpha_list) != self._modes:
+            raise ValueError("The number of alpha values must match the number of modes.")
+        from math import factorial
+
+        D = self._cutoff
+        vecs = [np.array([np.exp(-0.5 * abs(a) ** 2) * a ** k / np.sqrt(factorial(k)) for k in range(D)])
+                for a in alpha_list]
+        dev = self._tensor.device
+        if self._pure:
+            x = self._tensor.to(torch.complex128)
+            for v in vecs:
+                x = torch.tensordot(torch.as_tensor(v.conj(), device=dev), x, dims=([0], [0]))
+            return abs(x.item()) ** 2
+        x = self._tensor.to(torch.complex128)
+        for v in vecs:
+            vt = torch.as_tensor(v, device=dev)
+            x = torch.tensordot(vt.conj(), x, dims=([0], [0]))
+            x = torch.tensordot(vt, x, dims=([0], [0]))
+        return float(x.real.item())
+
+    # ----------------------------------------------------------------- quadratures
+    def quad_expectation(self, mode, phi=0, **kwargs):
+        """<x_phi> and Var(x_phi) of one mode (states.py:730)."""
+        D = self._cutoff
+        a = np.diag(np.sqrt(np.arange(1, D + 5)), 1)
+        x = np.sqrt(self._hbar / 2) * (a + a.T)
+        p = -1j * np.sqrt(self._hbar / 2) * (a - a.T)
+        xphi = np.cos(phi) * x + np.sin(phi) * p
+        xphisq = np.dot(xphi, xphi)
+        xphi = xphi[:D, :D]
+        xphisq = xphisq[:D, :D]
+        rho = self._rdm1(mode)
+        mean = np.trace(np.dot(xphi, rho)).real
+        var = np.trace(np.dot(xphisq, rho)).real - mean ** 2
+        return float(mean), float(var)
+
+    def number_expectation(self, modes):
+        values = np.arange(self._cutoff)
+        mean = self.diagonal_expectation(modes, values)
+        var = self.diagonal_expectation(modes, values ** 2) - mean ** 2
+        return mean, var
+
+    def parity_expectation(self, modes):
+        return self.diagonal_expectation(modes, (-1) ** np.arange(self._cutoff))
+
+    def diagonal_expectation(self, modes, values):
+        if len(modes) != len(set(modes)):
+            raise ValueError("There can be no duplicates in the modes specified.")
+        ps = self._probs_tensor()
+        traced = tuple(m for m in range(self._modes) if m not in modes)
+        if traced:
+            ps = ps.sum(dim=traced)
+        vt = torch.as_tensor(np.asarray(values, dtype=np.float64), device=ps.device)
+        for _ in modes:
+            ps = torch.tensordot(vt, ps, dims=1)
+        return float(ps.item())

@@ -1,0 +1,166 @@
+"""GPU compiled circuits (fused forward sweep) and adjoint gradients (rows
+A1-A3) against the oracle's tape adjoint, itself pinned to central finite
+differences in tests/test_oracle.py.
+
+Bars: complex128 state max abs error <= 1e-12 and gradient relative L2 error
+<= 1e-10; complex64 state <= 1e-5 and gradient relative L2 error <= 1e-5.
+"""
+import numpy as np
+import pytest
+
+from oracle import fock_oracle as fo
+
+pytestmark = pytest.mark.gpu
+
+# (kind, mode1, mode2, pidx) gate lists exercising every fusion rule
+MIXED_LIST = [
+    (1, 0, -1, 0),   # R before anything on mode 0 -> pre term of the BS
+    (2, 2, -1, 1),   # K on mode 2 -> pre term of the S2 (slot b)
+    (5, 0, 1, 2),
+    (4, 1, -1, 4),
+    (8, 0, 2, 6),    # cross-Kerr, flushed as its own op before S on 2
+    (4, 2, -1, 7),
+    (3, 0, -1, 9),
+    (2, 0, -1, 11),  # K after D on mode 0 -> post term (last op on mode 0 later? no: BS below)
+    (6, 2, 1, 12),   # S2 with swapped mode order
+    (7, 0, 2, 14),   # MZ on a non-adjacent pair
+    (8, 1, 2, 16),   # cross-Kerr fused into the next gate on the same pair
+    (5, 1, 2, 17),
+    (1, 1, -1, 19),  # trailing R on mode 1 -> post term of the last op on 1
+    (2, 2, -1, 20),
+]
+MIXED_NPARAMS = 21
+
+
+def _loss_grad(psi, t):
+    s = np.vdot(t, psi)
+    return 1 - abs(s) ** 2, -2 * s * t
+
+
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_fused_list_forward_and_gradient(cuda, dtype):
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+
+    N, D = 3, 6
+    rng = np.random.default_rng(7)
+    params = rng.uniform(0.05, 0.6, MIXED_NPARAMS)
+    tdt = torch.complex128 if dtype == "complex128" else torch.complex64
+    circ = CompiledCircuit(N, D, MIXED_LIST, MIXED_NPARAMS, dtype=tdt)
+    assert circ.n_ops < len(MIXED_LIST)
+    p = torch.tensor(params, device="cuda", requires_grad=True)
+    psi = circ(p)
+    ref_states = fo.run_gates(MIXED_LIST, params, N, D)
+    tol = 1e-12 if dtype == "complex128" else 1e-5
+    assert np.abs(psi.detach().to(torch.complex128).cpu().numpy() - ref_states[-1]).max() < tol
+    t = rng.normal(size=(D,) * N) + 1j * rng.normal(size=(D,) * N)
+    t /= np.linalg.norm(t)
+    tt = torch.as_tensor(t, device="cuda").to(tdt)
+    loss = 1 - torch.abs(torch.sum(tt.conj() * psi)) ** 2
+    loss.backward()
+    _, g_final = _loss_grad(ref_states[-1], t)
+    ref = fo.adjoint_grads(MIXED_LIST, params, N, D, g_final)
+    got = p.grad.cpu().numpy()
+    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert rel < (1e-10 if dtype == "complex128" else 1e-5), rel
+
+
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_qnn_forward_and_gradient(cuda, dtype):
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+    from strawberryfields_gb300.qnn import qnn_gates, qnn_params, target_state
+
+    N, D, layers = 4, 7, 2
+    gates, npar = qnn_gates(N, layers)
+    params = qnn_params(gates, npar, seed=3)
+    tdt = torch.complex128 if dtype == "complex128" else torch.complex64
+    circ = CompiledCircuit(N, D, gates, npar, dtype=tdt)
+    # diagonal gates are fused away: one op per non-diagonal gate
+    nd = sum(1 for g in gates if g[0] not in (1, 2, 8))
+    assert circ.n_ops == nd
+    p = torch.tensor(params, device="cuda", requires_grad=True)
+    psi = circ(p)
+    ref_states = fo.run_gates(gates, params, N, D)
+    tol = 1e-12 if dtype == "complex128" else 1e-5
+    assert np.abs(psi.detach().to(torch.complex128).cpu().numpy() - ref_states[-1]).max() < tol
+    t = target_state(N, D, 4, seed=5)
+    tt = torch.as_tensor(t, device="cuda").to(tdt)
+    loss = 1 - torch.abs(torch.sum(tt.conj() * psi)) ** 2
+    loss.backward()
+    ref = fo.adjoint_grads(gates, params, N, D, _loss_grad(ref_states[-1], t)[1])
+    got = p.grad.cpu().numpy()
+    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert rel < (1e-10 if dtype == "complex128" else 1e-5), rel
+
+
+def test_gradient_vs_central_differences_of_gpu_forward(cuda):
+    """The adjoint matches central differences of the GPU forward itself."""
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+    from strawberryfields_gb300.qnn import qnn_gates, qnn_params, target_state
+
+    N, D = 3, 6
+    gates, npar = qnn_gates(N, 1)
+    params = qnn_params(gates, npar, seed=11)
+    circ = CompiledCircuit(N, D, gates, npar, dtype=torch.complex128)
+    t = torch.as_tensor(target_state(N, D, 3, seed=2), device="cuda")
+
+    def loss(pv):
+        psi = circ.forward_states(torch.tensor(pv, device="cuda"), store_all=False)
+        return float((1 - torch.abs(torch.sum(t.conj() * psi)) ** 2).item())
+
+    p = torch.tensor(params, device="cuda", requires_grad=True)
+    psi = circ(p)
+    (1 - torch.abs(torch.sum(t.conj() * psi)) ** 2).backward()
+    h = 1e-6
+    fd = np.array([(loss(params + h * e) - loss(params - h * e)) / (2 * h) for e in np.eye(npar)])
+    assert np.abs(p.grad.cpu().numpy() - fd).max() < 1e-8
+
+
+def test_known_gradients_beamsplitter_on_11(cuda):
+    """Closed forms of the reference's TF gradient tests
+    (tests/integration/test_tf_integration.py: BS on |1,1>):
+    dP11/dtheta = -4 sin(2 theta) cos(2 theta), dP02/dtheta = sin(4 theta)."""
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+
+    D = 4
+    theta = 0.37
+    circ = CompiledCircuit(2, D, [(5, 0, 1, 0)], 2, dtype=torch.complex128)
+    psi0 = torch.zeros((D, D), dtype=torch.complex128, device="cuda")
+    psi0[1, 1] = 1.0
+    for idx, ref in [((1, 1), -4 * np.sin(2 * theta) * np.cos(2 * theta)), ((0, 2), np.sin(4 * theta))]:
+        p = torch.tensor([theta, 0.0], device="cuda", requires_grad=True)
+        psi = circ(p, state_in=psi0)
+        prob = torch.abs(psi[idx]) ** 2
+        prob.backward()
+        assert abs(p.grad[0].item() - ref) < 1e-12
+
+
+def test_known_gradient_two_mode_squeeze_vacuum(cuda):
+    """dP00/dr = -2 tanh(r) / cosh(r)^2 for S2(r)|00> (test_tf_integration.py)."""
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+
+    r = 0.21
+    circ = CompiledCircuit(2, 6, [(6, 0, 1, 0)], 2, dtype=torch.complex128)
+    p = torch.tensor([r, 0.3], device="cuda", requires_grad=True)
+    psi = circ(p)
+    (torch.abs(psi[0, 0]) ** 2).backward()
+    assert abs(p.grad[0].item() + 2 * np.tanh(r) / np.cosh(r) ** 2) < 1e-12
+
+
+def test_known_gradient_displacement_mean_photon(cuda):
+    """d<n>/dr = 2 r for a coherent state (high cutoff), d/dphi = 0."""
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+
+    D, r = 20, 0.4
+    circ = CompiledCircuit(1, D, [(3, 0, -1, 0)], 2, dtype=torch.complex128)
+    p = torch.tensor([r, 0.8], device="cuda", requires_grad=True)
+    psi = circ(p)
+    n = torch.arange(D, device="cuda", dtype=torch.float64)
+    (torch.sum(n * torch.abs(psi) ** 2)).backward()
+    assert abs(p.grad[0].item() - 2 * r) < 1e-9
+    assert abs(p.grad[1].item()) < 1e-12
