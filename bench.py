@@ -249,13 +249,10 @@ def gpu_arm(args, rank, world, cpu_base):
     clk = clocks.stop()
     _lib.check(lib.fock_plan_enable_timing(circ._plan, 0))
     step_ms = [a.elapsed_time(b) for a, b in evs]
-    my_ms = float(np.sum(step_ms))
-    if world > 1:
-        tt = torch.tensor([my_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        my_ms = float(tt.item())
+    from strawberryfields_gb300.replicas import job_throughput
+
+    value, my_ms = job_throughput(float(np.sum(step_ms)), args.steps)
     ms_per_step = my_ms / args.steps
-    value = world * args.steps / (my_ms / 1e3)
 
     # per-op kernel roofline (averages over the timed steps)
     fwd_ms /= args.steps
@@ -450,6 +447,7 @@ def main():
     if world > 1:
         import torch
 
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         torch.distributed.init_process_group("nccl")
     out = gpu_arm(args, rank, world, cpu_base)
     if rank == 0:

@@ -83,6 +83,7 @@ class FockGB300Backend:
     short_name = "fock_gb300"
     circuit_spec = "fock"
     compiler = "fock"
+    _state_cls = FockStateGB300
 
     def __init__(self):
         self._supported = {"mixed_states": True, "fock_basis": True}
@@ -227,7 +228,7 @@ class FockGB300Backend:
         cutoff = self.circuit._trunc
         if modes is None:
             names = ["q[{}]".format(i) for i in self.get_modes()]
-            return FockStateGB300(s, num, pure, cutoff, names)
+            return self._state_cls(s, num, pure, cutoff, names)
         if isinstance(modes, int):
             modes = [modes]
         if len(modes) != len(set(modes)):
@@ -244,7 +245,7 @@ class FockGB300Backend:
             red = np.transpose(red, np.argsort(idx))
         names = ["q[{}]".format(i) for i in np.array(self.get_modes())[modes]]
         t = torch.as_tensor(np.ascontiguousarray(red), device=s.device).to(s.dtype)
-        return FockStateGB300(t, len(modes), False, cutoff, names)
+        return self._state_cls(t, len(modes), False, cutoff, names)
 
 
 _SF_CLASS = None
@@ -256,8 +257,11 @@ def sf_backend():
     global _SF_CLASS
     if _SF_CLASS is None:
         from strawberryfields.backends.base import BaseFock  # pylint: disable=import-outside-toplevel
+        from strawberryfields.backends.states import BaseFockState  # pylint: disable=import-outside-toplevel
 
-        _SF_CLASS = type("FockGB300Backend", (FockGB300Backend, BaseFock), {})
+        # results carry the state only if it is a BaseState (strawberryfields/result.py)
+        state_cls = type("FockStateGB300", (FockStateGB300, BaseFockState), {})
+        _SF_CLASS = type("FockGB300Backend", (FockGB300Backend, BaseFock), {"_state_cls": state_cls})
     return _SF_CLASS()
 
 

@@ -1,0 +1,153 @@
+"""The C-ABI library without a GPU: it builds, loads, exports every symbol the
+header declares, validates arguments before touching the device, and its
+host-side circuit compiler (gate fusion) behaves as documented."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "fock_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from strawberryfields_gb300 import _lib
+    from strawberryfields_gb300 import build as b
+
+    if not os.path.exists(_lib.LIBPATH):
+        b.build()
+    return _lib.load()
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(fock_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_and_binding_agree():
+    from strawberryfields_gb300 import _lib
+
+    assert declared_functions() == _lib.exported_symbols()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_size_queries(lib):
+    from oracle import fock_oracle as fo  # noqa: F401  (checker import only)
+
+    assert lib.fock_gate_matrix_entries(3, 12) == 144
+    assert lib.fock_gate_matrix_entries(5, 12) == 12 * (2 * 144 + 1) // 3
+    assert lib.fock_gate_matrix_entries(6, 4) == sum(min(k, 8 - k) ** 2 for k in range(1, 8))
+    assert lib.fock_gate_matrix_entries(42, 12) == 0
+    assert lib.fock_gate_matrix_entries(3, 0) == 0
+    assert lib.fock_gate_workspace_bytes(4, 10) > 2 * 100 * 16
+
+
+def test_invalid_arguments_rejected_on_host(lib):
+    from strawberryfields_gb300 import _lib
+
+    dummy = ctypes.c_void_p(16)
+    # unknown kind, bad mode, bad cutoff, bad dtype, in == out: all caught before any CUDA call
+    cases = [
+        (42, 0, -1, 2, 4, 1, 0),
+        (3, 5, -1, 2, 4, 1, 0),
+        (3, 0, -1, 2, 0, 1, 0),
+        (3, 0, -1, 2, 4, 1, 7),
+        (5, 0, 0, 2, 4, 1, 0),
+    ]
+    for kind, m1, m2, n, D, pure, dt in cases:
+        rc = lib.fock_apply_gate(kind, 0.1, 0.0, m1, m2, n, D, pure, dt, None, dummy, ctypes.c_void_p(32), None,
+                                 dummy, None)
+        assert rc == _lib.FOCK_ERR_INVALID
+        assert _lib.last_error()
+    rc = lib.fock_apply_gate(3, 0.1, 0.0, 0, -1, 2, 4, 1, 0, None, dummy, dummy, None, dummy, None)
+    assert rc == _lib.FOCK_ERR_INVALID and "distinct" in _lib.last_error()
+    # loss on a pure state is refused (the host mixes first)
+    rc = lib.fock_apply_gate(9, 0.5, 0.0, 0, -1, 2, 4, 1, 0, None, dummy, ctypes.c_void_p(32), None, dummy, None)
+    assert rc == _lib.FOCK_ERR_INVALID and "mixed" in _lib.last_error()
+    with pytest.raises(ValueError):
+        _lib.check(rc)
+
+
+def _plan(gates, n_params, N=3, D=6, pure=1, dtype=0):
+    from strawberryfields_gb300 import _lib
+
+    lib = _lib.load()
+    arr = (_lib.FockGate * max(len(gates), 1))()
+    for i, (k, a, b, p) in enumerate(gates):
+        arr[i].kind, arr[i].mode1, arr[i].mode2, arr[i].pidx = k, a, b, p
+    plan = ctypes.c_void_p()
+    rc = lib.fock_plan_create(N, D, pure, dtype, arr, len(gates), n_params, ctypes.byref(plan))
+    return rc, plan
+
+
+def _ops(plan):
+    from strawberryfields_gb300 import _lib
+
+    lib = _lib.load()
+    info = _lib.PlanInfo()
+    assert lib.fock_plan_get_info(plan, ctypes.byref(info)) == 0
+    out = []
+    for k in range(info.n_ops):
+        a, b, c, d = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        assert lib.fock_plan_op(plan, k, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d)) == 0
+        out.append((a.value, b.value, c.value, d.value))
+    return info, out
+
+
+def test_plan_fuses_diagonal_gates(lib):
+    """Rotation/Kerr/cross-Kerr never get their own pass when a neighbour exists."""
+    from strawberryfields_gb300.qnn import qnn_gates
+
+    gates, npar = qnn_gates(6, 4)
+    rc, plan = _plan(gates, npar, N=6, D=12)
+    assert rc == 0
+    info, ops = _ops(plan)
+    nondiag = [g for g in gates if g[0] not in (1, 2, 8)]
+    assert info.n_ops == len(nondiag) == 168
+    assert sum(o[3] for o in ops) == len(gates)  # every gate accounted for once
+    assert info.state_bytes == 12 ** 6 * 8
+    assert info.bytes_fwd == 2 * info.state_bytes * 168
+    lib.fock_plan_destroy(plan)
+
+
+def test_plan_fusion_edge_cases(lib):
+    # R on a mode no other gate touches -> its own identity op; CK not followed
+    # by a gate on its pair -> its own op; trailing K -> output term of the last op
+    gates = [(1, 2, -1, 0), (5, 0, 1, 1), (8, 0, 1, 3), (2, 0, -1, 4), (4, 1, -1, 5)]
+    rc, plan = _plan(gates, 7)
+    assert rc == 0
+    info, ops = _ops(plan)
+    kinds = [(o[0], o[1], o[2]) for o in ops]
+    assert (2, 0, 1) in kinds          # BS (number-sum blocks)
+    assert (1, 1, -1) in kinds         # squeezer (dense)
+    assert (2, 0, 1) in kinds[1:] or sum(1 for k in kinds if k == (2, 0, 1)) == 2  # CK identity op
+    assert (1, 2, -1) in kinds         # identity op carrying R on mode 2
+    assert sum(o[3] for o in ops) == len(gates)
+    lib.fock_plan_destroy(plan)
+
+
+def test_plan_rejects_bad_gate_lists(lib):
+    from strawberryfields_gb300 import _lib
+
+    for gates, npar in [([(3, 4, -1, 0)], 2), ([(5, 0, 0, 0)], 2), ([(3, 0, -1, 1)], 2), ([(42, 0, -1, 0)], 2)]:
+        rc, plan = _plan(gates, npar)
+        assert rc == _lib.FOCK_ERR_INVALID
+    rc, plan = _plan([(3, 0, -1, 0)], 2, pure=0)
+    assert rc == _lib.FOCK_ERR_UNSUPPORTED
+
+
+def test_product_path_has_no_cpu_fallback():
+    """The package never imports the oracle."""
+    pkg = os.path.join(ROOT, "strawberryfields_gb300")
+    for fn in os.listdir(pkg):
+        if fn.endswith(".py"):
+            src = open(os.path.join(pkg, fn)).read()
+            assert "oracle" not in re.sub(r"#.*|\"\"\"[\s\S]*?\"\"\"", "", src), fn

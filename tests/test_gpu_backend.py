@@ -177,7 +177,7 @@ def test_gate_sequence_matches_oracle(cuda, pure, dtype):
     got = st.ket() if pure else st.dm()
     assert np.abs(got.astype(np.complex128) - ref).max() < tol
     # readouts
-    assert abs(st.trace() - (np.vdot(ref, ref).real if pure else fo.all_fock_probs(ref, N, False).sum())) < 1e-9
+    assert abs(st.trace() - (np.vdot(ref, ref).real if pure else fo.all_fock_probs(ref, N, False).sum())) < 100 * tol
     for m in range(N):
         mean, var = st.mean_photon(m)
         rm, rv = fo.mean_photon(ref, N, m, pure)

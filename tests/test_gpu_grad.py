@@ -131,7 +131,7 @@ def test_known_gradients_beamsplitter_on_11(cuda):
     psi0 = torch.zeros((D, D), dtype=torch.complex128, device="cuda")
     psi0[1, 1] = 1.0
     for idx, ref in [((1, 1), -4 * np.sin(2 * theta) * np.cos(2 * theta)), ((0, 2), np.sin(4 * theta))]:
-        p = torch.tensor([theta, 0.0], device="cuda", requires_grad=True)
+        p = torch.tensor([theta, 0.0], device="cuda", dtype=torch.float64, requires_grad=True)
         psi = circ(p, state_in=psi0)
         prob = torch.abs(psi[idx]) ** 2
         prob.backward()
@@ -145,7 +145,7 @@ def test_known_gradient_two_mode_squeeze_vacuum(cuda):
 
     r = 0.21
     circ = CompiledCircuit(2, 6, [(6, 0, 1, 0)], 2, dtype=torch.complex128)
-    p = torch.tensor([r, 0.3], device="cuda", requires_grad=True)
+    p = torch.tensor([r, 0.3], device="cuda", dtype=torch.float64, requires_grad=True)
     psi = circ(p)
     (torch.abs(psi[0, 0]) ** 2).backward()
     assert abs(p.grad[0].item() + 2 * np.tanh(r) / np.cosh(r) ** 2) < 1e-12
@@ -158,7 +158,7 @@ def test_known_gradient_displacement_mean_photon(cuda):
 
     D, r = 20, 0.4
     circ = CompiledCircuit(1, D, [(3, 0, -1, 0)], 2, dtype=torch.complex128)
-    p = torch.tensor([r, 0.8], device="cuda", requires_grad=True)
+    p = torch.tensor([r, 0.8], device="cuda", dtype=torch.float64, requires_grad=True)
     psi = circ(p)
     n = torch.arange(D, device="cuda", dtype=torch.float64)
     (torch.sum(n * torch.abs(psi) ** 2)).backward()

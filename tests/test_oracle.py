@@ -1,0 +1,177 @@
+"""Pins of the CPU oracle (no GPU).
+
+* gate matrices against scipy.linalg.expm of each generator (large cutoff,
+  truncated) -- the restated thewalrus builders;
+* the reference's analytic known answers (tests/backend in the reference);
+* FP64 derivative matrices and the tape adjoint against central differences;
+* the oracle's state updates against the reference's own Circuit (when the
+  reference sources are present) and against the committed golden vectors.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+from scipy.linalg import expm
+
+from oracle import fock_oracle as fo
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def a_op(D):
+    return np.diag(np.sqrt(np.arange(1, D, dtype=float)), 1).astype(complex)
+
+
+@pytest.mark.parametrize("r,phi", [(0.0, 0.0), (0.37, 1.1), (0.8, -2.3)])
+def test_displacement_squeezing_vs_expm(r, phi):
+    Db, D = 70, 12
+    a = a_op(Db)
+    ad = a.conj().T
+    al = r * np.exp(1j * phi)
+    assert np.abs(expm(al * ad - np.conj(al) * a)[:D, :D] - fo.displacement(r, phi, D)).max() < 1e-13
+    Sm = expm(0.5 * (np.conj(al) * a @ a - al * ad @ ad))[:D, :D]
+    assert np.abs(Sm - fo.squeezing(r, phi, D)).max() < 1e-13
+
+
+@pytest.mark.parametrize("p0,p1", [(0.7, 1.3), (1.2, -0.4)])
+def test_two_mode_gates_vs_expm(p0, p1):
+    Db, D = 26, 7
+    a = a_op(Db)
+    I = np.eye(Db)
+    a1, a2 = np.kron(a, I), np.kron(I, a)
+
+    def sf_order(U):
+        return U.reshape(Db, Db, Db, Db)[:D, :D, :D, :D].transpose(0, 2, 1, 3)
+
+    B = expm(p0 * (np.exp(1j * p1) * a1 @ a2.conj().T - np.exp(-1j * p1) * a1.conj().T @ a2))
+    assert np.abs(sf_order(B) - fo.beamsplitter(p0, p1, D)).max() < 1e-13
+    r = p0 / 3
+    z = r * np.exp(1j * p1)
+    S2 = expm(z * a1.conj().T @ a2.conj().T - np.conj(z) * a1 @ a2)
+    assert np.abs(sf_order(S2) - fo.two_mode_squeeze(r, p1, D)).max() < 1e-12
+    R1 = lambda p: expm(1j * p * a1.conj().T @ a1)  # noqa: E731
+    B50 = expm(np.pi / 4 * (np.exp(1j * np.pi / 2) * a1 @ a2.conj().T - np.exp(-1j * np.pi / 2) * a1.conj().T @ a2))
+    MZ = B50 @ R1(p0) @ B50 @ R1(p1)
+    assert np.abs(sf_order(MZ) - fo.mzgate(p0, p1, D)).max() < 1e-12
+
+
+def test_known_answers():
+    D = 12
+    # coherent column (test_displacement_operation.py)
+    al = 0.3 * np.exp(0.4j)
+    k = np.arange(D)
+    fac = np.array([math.factorial(int(i)) for i in k], dtype=float)
+    coh = np.exp(-0.5 * abs(al) ** 2) * al ** k / np.sqrt(fac)
+    assert np.abs(fo.displacement(abs(al), np.angle(al), D)[:, 0] - coh).max() < 1e-15
+    # squeezed vacuum (Loudon 5.5.6)
+    r, phi = 0.4, 0.9
+    sv = np.zeros(D, dtype=complex)
+    for n in range(0, D, 2):
+        m = n // 2
+        sv[n] = math.sqrt(math.factorial(2 * m)) / (2 ** m * math.factorial(m)) * (-np.exp(1j * phi) * np.tanh(r)) ** m
+    assert np.abs(fo.squeezing(r, phi, D)[:, 0] - sv / math.sqrt(math.cosh(r))).max() < 1e-15
+    # TMSV
+    T = fo.two_mode_squeeze(r, phi, D)
+    for n in range(D):
+        assert abs(T[n, 0, n, 0] - (np.exp(1j * phi) * np.tanh(r)) ** n / np.cosh(r)) < 1e-15
+    # beamsplitter on |alpha, 0> -> |t alpha, r alpha> (photon number < D exactly representable)
+    th, ph = 0.6, 1.2
+    psi = fo.apply_gate2(np.multiply.outer(fo.coherent_state(0.3, 0.0, D), fo.vacuum(1, D)), fo.beamsplitter(th, ph, D), 0, 1)
+    ref = np.multiply.outer(fo.coherent_state(0.3 * np.cos(th), 0.0, D),
+                            fo.coherent_state(0.3 * np.sin(th), ph, D))
+    assert np.abs(psi - ref).max() < 1e-9
+    # loss closed form against the Kraus sum
+    rho = np.random.default_rng(0).normal(size=(D, D)) + 0j
+    c = fo.loss_coeffs(0.8, D)
+    out = np.zeros_like(rho)
+    for n in range(D):
+        for m in range(D):
+            for l in range(min(n, m) + 1):
+                out[n - l, m - l] += c[n, m, l] * rho[n, m]
+    ref = sum(E @ rho @ E.conj().T for E in fo.loss_kraus(0.8, D))
+    assert np.abs(out - ref).max() < 1e-14
+
+
+def test_derivative_matrices_vs_central_differences():
+    h = 1e-6
+    for f, g, args in [(fo.displacement, fo.grad_displacement, (0.37, 1.1)),
+                       (fo.squeezing, fo.grad_squeezing, (0.37, 1.1)),
+                       (fo.beamsplitter, fo.grad_beamsplitter, (0.7, 1.1)),
+                       (fo.two_mode_squeeze, fo.grad_two_mode_squeeze, (0.37, 1.1))]:
+        d0, d1 = g(*args, 8)
+        fd0 = (f(args[0] + h, args[1], 8) - f(args[0] - h, args[1], 8)) / (2 * h)
+        fd1 = (f(args[0], args[1] + h, 8) - f(args[0], args[1] - h, 8)) / (2 * h)
+        assert np.abs(d0 - fd0).max() < 1e-8 and np.abs(d1 - fd1).max() < 1e-8
+
+
+def test_tape_adjoint_vs_central_differences():
+    N, D = 3, 6
+    gates = [(4, 0, -1, 0), (3, 1, -1, 2), (5, 0, 1, 4), (1, 2, -1, 6), (2, 1, -1, 7), (6, 1, 2, 8),
+             (7, 0, 2, 10), (8, 0, 1, 12), (5, 2, 1, 13), (3, 2, -1, 15)]
+    rng = np.random.default_rng(0)
+    params = rng.uniform(0.05, 0.5, 17)
+    t = rng.normal(size=(D,) * N) + 1j * rng.normal(size=(D,) * N)
+    t /= np.linalg.norm(t)
+
+    def loss(p):
+        s = np.vdot(t, fo.run_gates(gates, p, N, D)[-1])
+        return 1 - abs(s) ** 2
+
+    s = np.vdot(t, fo.run_gates(gates, params, N, D)[-1])
+    g = fo.adjoint_grads(gates, params, N, D, -2 * s * t)
+    h = 1e-6
+    fd = np.array([(loss(params + h * e) - loss(params - h * e)) / (2 * h) for e in np.eye(17)])
+    assert np.abs(g - fd).max() < 1e-9
+
+
+def _golden_cases():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+def oracle_run(N, D, pure, ops):
+    s = fo.vacuum(N, D, pure)
+    for op in ops:
+        name, rest = op[0], op[1:]
+        if name == "S":
+            s = fo.apply_gate1(s, fo.squeezing(rest[0], rest[1], D), rest[2], pure)
+        elif name == "D":
+            s = fo.apply_gate1(s, fo.displacement(rest[0], rest[1], D), rest[2], pure)
+        elif name == "R":
+            s = fo.apply_gate1(s, fo.phase(rest[0], D), rest[1], pure)
+        elif name == "K":
+            s = fo.apply_gate1(s, fo.kerr(rest[0], D), rest[1], pure)
+        elif name == "BS":
+            s = fo.apply_gate2(s, fo.beamsplitter(rest[0], rest[1], D), rest[2], rest[3], pure)
+        elif name == "S2":
+            s = fo.apply_gate2(s, fo.two_mode_squeeze(rest[0], rest[1], D), rest[2], rest[3], pure)
+        elif name == "MZ":
+            s = fo.apply_gate2(s, fo.mzgate(rest[0], rest[1], D), rest[2], rest[3], pure)
+        elif name == "CK":
+            s = fo.apply_gate2(s, fo.cross_kerr(rest[0], D), rest[1], rest[2], pure)
+        elif name == "L":
+            s = fo.apply_loss(s, rest[0], rest[1], N, pure)
+            pure = False
+    return s
+
+
+@pytest.mark.parametrize("case", _golden_cases())
+def test_oracle_reproduces_golden(case):
+    from tests.golden.make_golden import decode
+
+    z = np.load(os.path.join(GOLDEN, case + ".npz"))
+    got = oracle_run(int(z["N"]), int(z["D"]), bool(z["pure"]), decode(z["ops"]))
+    assert np.abs(got - z["state"]).max() < 1e-13
+
+
+def test_oracle_vs_reference_circuit():
+    """Regenerate one golden case through the reference Circuit directly."""
+    from oracle import sfref
+
+    if sfref.find_reference() is None:
+        pytest.skip("reference sources not present")
+    from tests.golden import make_golden as mg
+
+    N, D, pure, ops = mg.pure_all(1)
+    ref, _ = mg.run_reference(N, D, pure, ops)
+    assert np.abs(oracle_run(N, D, pure, ops) - ref).max() < 1e-13
