@@ -139,6 +139,19 @@ int fock_reduced_dm1(int num_modes, int cutoff, int pure, int dtype, int mode, c
                      void* out, void* workspace, void* stream);
 int64_t fock_reduced_dm1_workspace_bytes(int num_modes, int cutoff, int pure, int dtype);
 
+/* Same result as fock_reduced_dm1, for callers that cannot allocate device
+ * memory (no workspace argument).  No counterpart in the reference.  The
+ * reduction's partial sums live in a fixed 512 KiB array in device global
+ * memory owned by the library (held by every GPU that loads it until exit),
+ * which bounds the cutoff to <= 60; larger cutoffs are rejected with
+ * FOCK_ERR_INVALID.  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress) with the device current: make that first
+ * call before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU (different streams, or concurrent host threads) race;
+ * serialise them.  Allocates nothing: no cudaMalloc/cudaFree. */
+int fock_reduced_dm1_noalloc(int num_modes, int cutoff, int pure, int dtype, int mode, const void* state,
+                             void* out, void* stream);
+
 /* ---------------------------------------------- compiled circuits + adjoint (A1-A3)
  * A plan is a gate list compiled on the host: rotation/Kerr/cross-Kerr gates
  * are fused into the neighbouring non-diagonal gate, so the state crosses HBM

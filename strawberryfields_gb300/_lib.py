@@ -73,6 +73,7 @@ _SIGS = {
     "fock_marginals_workspace_bytes": (_i64, [_i, _i, _i, _i]),
     "fock_reduced_dm1": (_i, [_i, _i, _i, _i, _i, _vp, _vp, _vp, _vp]),
     "fock_reduced_dm1_workspace_bytes": (_i64, [_i, _i, _i, _i]),
+    "fock_reduced_dm1_noalloc": (_i, [_i, _i, _i, _i, _i, _vp, _vp, _vp]),
     "fock_plan_create": (_i, [_i, _i, _i, _i, ctypes.POINTER(FockGate), _i, _i, ctypes.POINTER(_vp)]),
     "fock_plan_destroy": (None, [_vp]),
     "fock_plan_get_info": (_i, [_vp, ctypes.POINTER(PlanInfo)]),

@@ -95,6 +95,13 @@ int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* 
 int64_t adjoint_scratch_entries(int dtype, const AxisView& v, int D, int layout);
 int adjoint_grid_x(int dtype, const AxisView& v, int D, int layout);
 
+// reduced density matrix pieces (capi.cu)
+int launch_rdm_mixed(int dtype, const void* state, int num_modes, int D, int mode, int64_t ntr, int chunks,
+                     double2* part, cudaStream_t st);
+int launch_transpose_dm(const double2* C, double2* out, int D, cudaStream_t st);
+int check_reduced_dm1_args(int num_modes, int cutoff, int pure, int dtype, int mode, const void* state,
+                           const void* out);
+
 // single matrix build with inline parameters (gates.cu)
 int build_single(int gate, int layout, int D, double p0, double p1, const PhaseTerm* terms,
                  int nterm, double2* M, double2* dM, double2* scratch, cudaStream_t st);

@@ -600,6 +600,33 @@ __global__ void transpose_dm_kernel(const double2* __restrict__ c, double2* __re
   }
 }
 
+int launch_rdm_mixed(int dtype, const void* state, int num_modes, int D, int mode, int64_t ntr, int chunks,
+                     double2* part, cudaStream_t st) {
+  dim3 grid(D * D, chunks);
+  if (dtype == FOCK_C64)
+    rdm_mixed_kernel<float2><<<grid, 256, 0, st>>>((const float2*)state, num_modes, D, mode, ntr, part);
+  else
+    rdm_mixed_kernel<double2><<<grid, 256, 0, st>>>((const double2*)state, num_modes, D, mode, ntr, part);
+  FOCK_LAUNCH_CHECK("rdm_mixed_kernel");
+  return FOCK_OK;
+}
+
+int launch_transpose_dm(const double2* C, double2* out, int D, cudaStream_t st) {
+  transpose_dm_kernel<<<1, 256, 0, st>>>(C, out, D);
+  FOCK_LAUNCH_CHECK("transpose_dm_kernel");
+  return FOCK_OK;
+}
+
+int check_reduced_dm1_args(int num_modes, int cutoff, int pure, int dtype, int mode, const void* state,
+                           const void* out) {
+  int64_t n;
+  int rc = check_state(num_modes, cutoff, pure, dtype, &n);
+  if (rc) return rc;
+  if ((rc = check_mode(mode, num_modes, "mode"))) return rc;
+  if (!state || !out) return fock_set_error(FOCK_ERR_INVALID, "null buffer");
+  return FOCK_OK;
+}
+
 extern "C" int64_t fock_reduced_dm1_workspace_bytes(int num_modes, int cutoff, int pure, int dtype) {
   int64_t c = (int64_t)cutoff * cutoff;
   if (pure) {
