@@ -170,11 +170,18 @@ typedef struct fock_plan_info {
   int64_t state_bytes;
   int64_t workspace_bytes;  /* for forward and backward */
   int64_t flops_fwd;        /* real flops of one forward */
-  int64_t bytes_fwd;        /* algorithmic HBM bytes of one forward (2 S per op) */
+  int64_t bytes_fwd;        /* algorithmic HBM bytes of one forward (2 S per op, whole batch) */
+  int32_t batch;            /* circuits per call */
 } fock_plan_info;
 
 int fock_plan_create(int num_modes, int cutoff, int pure, int dtype, const fock_gate* gates,
                      int n_gates, int n_params, fock_plan** out);
+/* A batch of `batch` circuits with this gate list, each with its own
+ * parameters -- the batch axis of the reference's TF backend
+ * (tfbackend/circuit.py:129-185).  params: [batch][n_params]; state_in:
+ * [batch][D^n]; states: [n_ops or 2][batch][D^n]; gradients likewise. */
+int fock_plan_create_batch(int num_modes, int cutoff, int pure, int dtype, const fock_gate* gates,
+                           int n_gates, int n_params, int batch, fock_plan** out);
 void fock_plan_destroy(fock_plan* plan);
 int fock_plan_get_info(const fock_plan* plan, fock_plan_info* info);
 /* Fused op k: kind code (1 dense single-mode, 2 number-sum block, 3

@@ -44,7 +44,7 @@ class FockGate(ctypes.Structure):
 class PlanInfo(ctypes.Structure):
     _fields_ = [("n_ops", ctypes.c_int32), ("n_gates", ctypes.c_int32), ("state_elems", ctypes.c_int64),
                 ("state_bytes", ctypes.c_int64), ("workspace_bytes", ctypes.c_int64),
-                ("flops_fwd", ctypes.c_int64), ("bytes_fwd", ctypes.c_int64)]
+                ("flops_fwd", ctypes.c_int64), ("bytes_fwd", ctypes.c_int64), ("batch", ctypes.c_int32)]
 
 
 _vp = ctypes.c_void_p
@@ -75,6 +75,7 @@ _SIGS = {
     "fock_reduced_dm1_workspace_bytes": (_i64, [_i, _i, _i, _i]),
     "fock_reduced_dm1_noalloc": (_i, [_i, _i, _i, _i, _i, _vp, _vp, _vp]),
     "fock_plan_create": (_i, [_i, _i, _i, _i, ctypes.POINTER(FockGate), _i, _i, ctypes.POINTER(_vp)]),
+    "fock_plan_create_batch": (_i, [_i, _i, _i, _i, ctypes.POINTER(FockGate), _i, _i, _i, ctypes.POINTER(_vp)]),
     "fock_plan_destroy": (None, [_vp]),
     "fock_plan_get_info": (_i, [_vp, ctypes.POINTER(PlanInfo)]),
     "fock_plan_op": (_i, [_vp, _i, _ip, _ip, _ip, _ip]),

@@ -36,9 +36,13 @@ class CompiledCircuit:
         n_params (int): length of the parameter vector
         dtype: ``torch.complex64`` (default) or ``torch.complex128`` state
         device: CUDA device
+        batch (int): number of circuits of this structure run together, each
+            with its own parameters (parameters ``[batch, n_params]``, states
+            ``[batch, D, ..., D]``) -- the batch axis of the reference's TF
+            backend (``tfbackend/circuit.py:129-185``); 1 gives unbatched shapes
     """
 
-    def __init__(self, num_modes, cutoff, gates, n_params, dtype=torch.complex64, device=None):
+    def __init__(self, num_modes, cutoff, gates, n_params, dtype=torch.complex64, device=None, batch=1):
         lib = L.load()
         self.num_modes = int(num_modes)
         self.cutoff = int(cutoff)
@@ -50,17 +54,20 @@ class CompiledCircuit:
             kind, m1, m2, pidx = g
             arr[i].kind, arr[i].mode1, arr[i].mode2, arr[i].pidx = int(kind), int(m1), int(m2), int(pidx)
         plan = ctypes.c_void_p()
-        L.check(lib.fock_plan_create(self.num_modes, self.cutoff, 1, self._dcode, arr, len(gates), self.n_params,
-                                     ctypes.byref(plan)), "fock_plan_create")
+        self.batch = int(batch)
+        L.check(lib.fock_plan_create_batch(self.num_modes, self.cutoff, 1, self._dcode, arr, len(gates),
+                                           self.n_params, self.batch, ctypes.byref(plan)), "fock_plan_create")
         self._plan = plan
         info = L.PlanInfo()
         L.check(lib.fock_plan_get_info(plan, ctypes.byref(info)), "fock_plan_get_info")
         self.info = info
         self.n_gates = len(gates)
         self.shape = [self.cutoff] * self.num_modes
+        self._bshape = ([self.batch] if self.batch > 1 else []) + self.shape
         self._ws = torch.empty(int(info.workspace_bytes), dtype=torch.uint8, device=self.device)
-        self._vacuum = torch.zeros(self.shape, dtype=self.dtype, device=self.device)
-        self._vacuum.view(-1)[0] = 1.0
+        self._vacuum = torch.zeros([self.batch, int(info.state_elems)], dtype=self.dtype, device=self.device)
+        self._vacuum[:, 0] = 1.0
+        self._vacuum = self._vacuum.reshape(self._bshape)
 
     def __del__(self):
         plan = getattr(self, "_plan", None)
@@ -93,8 +100,8 @@ class CompiledCircuit:
         p = torch.as_tensor(params)
         if p.device != self.device or p.dtype != torch.float64:
             p = p.to(device=self.device, dtype=torch.float64)
-        if p.numel() != self.n_params:
-            raise ValueError(f"expected {self.n_params} parameters, got {p.numel()}")
+        if p.numel() != self.n_params * self.batch:
+            raise ValueError(f"expected {self.batch} x {self.n_params} parameters, got {tuple(p.shape)}")
         return p.contiguous()
 
     def forward_states(self, params, state_in=None, store_all=True):
@@ -107,7 +114,7 @@ class CompiledCircuit:
         if n == 0:
             return x.clone().unsqueeze(0)
         slots = n if store_all else min(n, 2)
-        states = torch.empty([slots] + self.shape, dtype=self.dtype, device=self.device)
+        states = torch.empty([slots] + self._bshape, dtype=self.dtype, device=self.device)
         L.check(L.load().fock_plan_forward(self._plan, p.data_ptr(), x.data_ptr(), states.data_ptr(),
                                            int(store_all), self._ws.data_ptr(), self._stream()),
                 "fock_plan_forward")
@@ -121,7 +128,8 @@ class CompiledCircuit:
         x = self._vacuum if state_in is None else state_in.to(self.dtype).contiguous()
         lam = grad_state.to(self.dtype).contiguous().clone()
         tmp = torch.empty_like(lam)
-        grads = torch.empty(self.n_params, dtype=torch.float64, device=self.device)
+        grads = torch.empty(([self.batch] if self.batch > 1 else []) + [self.n_params], dtype=torch.float64,
+                            device=self.device)
         if self.n_ops == 0:
             grads.zero_()
             return grads, lam

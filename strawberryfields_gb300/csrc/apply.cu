@@ -4,13 +4,16 @@
 // D x D block (single-mode gates) or as 2D-1 photon-number blocks (beamsplitter
 // / MZ conserve n1+n2, two-mode squeezing and the loss superoperator conserve
 // n1-n2 -- the selection rules the reference exploits in
-// fockbackend/circuit.py:307-365).  Grid: x over columns (one thread per
-// column), y over blocks.  Each thread loads the s values of its block into
+// fockbackend/circuit.py:307-365).  Grid: x over column pairs, y over blocks
+// (largest first).  Each thread takes two columns (j and j + 256 of its
+// CTA's 512-column slice): it loads the s values of its block for both into
 // registers (coalesced across the warp: consecutive threads take consecutive
 // columns, i.e. consecutive addresses along the innermost non-gate axis),
-// multiplies by the s x s block held in shared memory (broadcast reads) and
-// stores s outputs.  The block size s is a compile-time constant through a
-// switch, so the loads and the complex FMAs are fully unrolled.
+// multiplies by the s x s block held in shared memory -- every matrix entry
+// read from shared memory feeds both columns -- and stores 2 s outputs.  The
+// kernel is compiled per cutoff bucket DMAX so its register budget matches the
+// largest block it can meet; block sizes are compile-time constants through a
+// dispatch chain, so loads and complex FMAs are fully unrolled.
 #include "apply.cuh"
 
 AxisView make_view1(int naxes, int D, int ax) {
@@ -37,77 +40,123 @@ AxisView make_view2(int naxes, int D, int ax1, int ax2) {
   return v;
 }
 
+#define APPLY_THREADS 256
+#define APPLY_COLS 2
+
 template <typename CT, int S>
 __device__ __forceinline__ void apply_cols(const CT* __restrict__ in, CT* __restrict__ out,
                                            const AxisView& v, int D, const CT* Ms,
-                                           const BlockGeom& g, int64_t j) {
-  const int64_t base = col_base(v, j, D) + g.boff;
-  const CT* p = in + base;
-  CT x[S];
+                                           const BlockGeom& g, int64_t j0) {
+  const int64_t j1 = j0 + APPLY_THREADS;
+  const bool has1 = j1 < v.ncols;
+  const int64_t b0 = col_base(v, j0, D) + g.boff;
+  const int64_t b1 = has1 ? col_base(v, j1, D) + g.boff : b0;
+  CT x0[S], x1[S];
 #pragma unroll
-  for (int u = 0; u < S; ++u) x[u] = __ldg(p + u * g.step);
-  CT* q = out + base;
+  for (int u = 0; u < S; ++u) {
+    x0[u] = __ldg(in + b0 + u * g.step);
+    x1[u] = __ldg(in + b1 + u * g.step);
+  }
 #pragma unroll
   for (int w = 0; w < S; ++w) {
-    CT acc = czero<CT>();
+    CT a0 = czero<CT>(), a1 = czero<CT>();
 #pragma unroll
-    for (int u = 0; u < S; ++u) cfma(acc, Ms[w * S + u], x[u]);
-    q[w * g.step] = acc;
+    for (int u = 0; u < S; ++u) {
+      const CT m = Ms[w * S + u];
+      cfma(a0, m, x0[u]);
+      cfma(a1, m, x1[u]);
+    }
+    out[b0 + w * g.step] = a0;
+    if (has1) out[b1 + w * g.step] = a1;
   }
 }
 
 template <typename CT>
 __device__ void apply_cols_generic(const CT* __restrict__ in, CT* __restrict__ out, const AxisView& v,
-                                   int D, const CT* Ms, const BlockGeom& g, int64_t j) {
-  const int64_t base = col_base(v, j, D) + g.boff;
-  const int S = g.s;
-  for (int w = 0; w < S; ++w) {
-    CT acc = czero<CT>();
-    for (int u = 0; u < S; ++u) cfma(acc, Ms[w * S + u], in[base + u * g.step]);
-    out[base + w * g.step] = acc;
+                                   int D, const CT* Ms, const BlockGeom& g, int64_t j0) {
+  for (int k = 0; k < APPLY_COLS; ++k) {
+    const int64_t j = j0 + k * APPLY_THREADS;
+    if (j >= v.ncols) break;
+    const int64_t base = col_base(v, j, D) + g.boff;
+    const int S = g.s;
+    for (int w = 0; w < S; ++w) {
+      CT acc = czero<CT>();
+      for (int u = 0; u < S; ++u) cfma(acc, Ms[w * S + u], in[base + u * g.step]);
+      out[base + w * g.step] = acc;
+    }
   }
 }
 
-#define APPLY_CASE(N) case N: apply_cols<CT, N>(in, out, v, D, Ms, g, j); break;
+// s == S ? run the unrolled body : try S + 1 (up to DMAX)
+template <typename CT, int S, int DMAX>
+struct ApplyDispatch {
+  __device__ __forceinline__ static void run(const CT* in, CT* out, const AxisView& v, int D, const CT* Ms,
+                                             const BlockGeom& g, int64_t j0) {
+    if (g.s == S) apply_cols<CT, S>(in, out, v, D, Ms, g, j0);
+    else ApplyDispatch<CT, S + 1, DMAX>::run(in, out, v, D, Ms, g, j0);
+  }
+};
+template <typename CT, int DMAX>
+struct ApplyDispatch<CT, DMAX + 1, DMAX> {
+  __device__ __forceinline__ static void run(const CT* in, CT* out, const AxisView& v, int D, const CT* Ms,
+                                             const BlockGeom& g, int64_t j0) {
+    apply_cols_generic<CT>(in, out, v, D, Ms, g, j0);
+  }
+};
 
-template <typename CT>
-__global__ void __launch_bounds__(256) apply_block_kernel(const CT* __restrict__ in, CT* __restrict__ out,
-                                                          AxisView v, int D, int layout,
-                                                          const double2* __restrict__ mat, int mflags) {
+template <typename CT, int DMAX>
+__global__ void __launch_bounds__(APPLY_THREADS) apply_block_kernel(const CT* __restrict__ in,
+                                                                    CT* __restrict__ out, AxisView v, int D,
+                                                                    int layout,
+                                                                    const double2* __restrict__ mat,
+                                                                    int mflags, BatchArg bt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   CT* Ms = reinterpret_cast<CT*>(smem_raw);
-  const BlockGeom g = block_geom(v, D, layout, blockIdx.y, (mflags & MF_SWAP) ? 1 : 0);
+  in += blockIdx.z * bt.state_stride;
+  out += blockIdx.z * bt.state_stride;
+  mat += blockIdx.z * bt.mat_stride;
+  const int b = layout == LAYOUT_DENSE ? 0 : block_of_y(D, blockIdx.y);
+  const BlockGeom g = block_geom(v, D, layout, b, (mflags & MF_SWAP) ? 1 : 0);
   stage_block(Ms, mat, g, mflags);
   __syncthreads();
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= v.ncols) return;
-  switch (g.s) {
-    APPLY_CASE(1) APPLY_CASE(2) APPLY_CASE(3) APPLY_CASE(4) APPLY_CASE(5) APPLY_CASE(6)
-    APPLY_CASE(7) APPLY_CASE(8) APPLY_CASE(9) APPLY_CASE(10) APPLY_CASE(11) APPLY_CASE(12)
-    APPLY_CASE(13) APPLY_CASE(14) APPLY_CASE(15) APPLY_CASE(16) APPLY_CASE(17) APPLY_CASE(18)
-    APPLY_CASE(19) APPLY_CASE(20) APPLY_CASE(21) APPLY_CASE(22) APPLY_CASE(23) APPLY_CASE(24)
-    default: apply_cols_generic<CT>(in, out, v, D, Ms, g, j); break;
+  const int64_t j0 = (int64_t)blockIdx.x * (APPLY_THREADS * APPLY_COLS) + threadIdx.x;
+  if (j0 >= v.ncols) return;
+  ApplyDispatch<CT, 1, DMAX>::run(in, out, v, D, Ms, g, j0);
+}
+
+template <typename CT, int DMAX>
+static int launch_apply_t(const void* in, void* out, const AxisView& v, int D, int layout, const double2* mat,
+                          int mflags, cudaStream_t st, const BatchArg& bt) {
+  const int nblk = layout == LAYOUT_DENSE ? 1 : 2 * D - 1;
+  const int64_t gx = (v.ncols + APPLY_THREADS * APPLY_COLS - 1) / (APPLY_THREADS * APPLY_COLS);
+  if (gx > 0x7fffffffLL) return fock_set_error(FOCK_ERR_INVALID, "state too large");
+  if (bt.nb < 1 || bt.nb > 65535) return fock_set_error(FOCK_ERR_INVALID, "batch of %d circuits", bt.nb);
+  dim3 grid((unsigned)gx, nblk, bt.nb);
+  const size_t sm = (size_t)D * D * sizeof(CT);
+  auto k = apply_block_kernel<CT, DMAX>;
+  if (sm > 48 * 1024) FOCK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  k<<<grid, APPLY_THREADS, sm, st>>>((const CT*)in, (CT*)out, v, D, layout, mat, mflags, bt);
+  FOCK_LAUNCH_CHECK("apply_block_kernel");
+  return FOCK_OK;
+}
+
+template <typename CT>
+static int launch_apply_d(const void* in, void* out, const AxisView& v, int D, int layout, const double2* mat,
+                          int mflags, cudaStream_t st, const BatchArg& bt) {
+  switch (dmax_bucket(D)) {
+    case 4: return launch_apply_t<CT, 4>(in, out, v, D, layout, mat, mflags, st, bt);
+    case 8: return launch_apply_t<CT, 8>(in, out, v, D, layout, mat, mflags, st, bt);
+    case 12: return launch_apply_t<CT, 12>(in, out, v, D, layout, mat, mflags, st, bt);
+    case 16: return launch_apply_t<CT, 16>(in, out, v, D, layout, mat, mflags, st, bt);
+    case 20: return launch_apply_t<CT, 20>(in, out, v, D, layout, mat, mflags, st, bt);
+    case 24: return launch_apply_t<CT, 24>(in, out, v, D, layout, mat, mflags, st, bt);
+    default: return launch_apply_t<CT, 0>(in, out, v, D, layout, mat, mflags, st, bt);
   }
 }
 
 int launch_apply(int dtype, const void* in, void* out, const AxisView& v, int D, int layout,
-                 const double2* mat, int mflags, cudaStream_t st) {
+                 const double2* mat, int mflags, cudaStream_t st, const BatchArg& bt) {
   if (v.ncols <= 0) return FOCK_OK;
-  const int nblk = layout == LAYOUT_DENSE ? 1 : 2 * D - 1;
-  const int64_t gx = (v.ncols + 255) / 256;
-  if (gx > 0x7fffffffLL) return fock_set_error(FOCK_ERR_INVALID, "state too large");
-  dim3 grid((unsigned)gx, nblk);
-  if (dtype == FOCK_C64) {
-    size_t sm = (size_t)D * D * sizeof(float2);
-    if (sm > 48 * 1024)
-      FOCK_CUDA_TRY(cudaFuncSetAttribute(apply_block_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    apply_block_kernel<float2><<<grid, 256, sm, st>>>((const float2*)in, (float2*)out, v, D, layout, mat, mflags);
-  } else {
-    size_t sm = (size_t)D * D * sizeof(double2);
-    if (sm > 48 * 1024)
-      FOCK_CUDA_TRY(cudaFuncSetAttribute(apply_block_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    apply_block_kernel<double2><<<grid, 256, sm, st>>>((const double2*)in, (double2*)out, v, D, layout, mat, mflags);
-  }
-  FOCK_LAUNCH_CHECK("apply_block_kernel");
-  return FOCK_OK;
+  if (dtype == FOCK_C64) return launch_apply_d<float2>(in, out, v, D, layout, mat, mflags, st, bt);
+  return launch_apply_d<double2>(in, out, v, D, layout, mat, mflags, st, bt);
 }

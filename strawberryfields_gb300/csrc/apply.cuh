@@ -37,6 +37,18 @@ struct BlockGeom {
   int rev;        // stored position = s-1-u (swapped SUM blocks)
 };
 
+// Grid position y -> block index, largest blocks first (sizes D, D-1, D-1,
+// D-2, D-2, ...), so the hardware scheduler starts the longest work first.
+__host__ __device__ __forceinline__ int block_of_y(int D, int y) {
+  return (D - 1) + ((y & 1) ? -((y + 1) >> 1) : (y >> 1));
+}
+
+// Cutoff bucket a kernel instance is compiled for (block sizes 1..DMAX run
+// fully unrolled from registers; 0 = generic loop kernel for larger cutoffs).
+__host__ __device__ __forceinline__ int dmax_bucket(int D) {
+  return D <= 4 ? 4 : D <= 8 ? 8 : D <= 12 ? 12 : D <= 16 ? 16 : D <= 20 ? 20 : D <= 24 ? 24 : 0;
+}
+
 __device__ __forceinline__ BlockGeom block_geom(const AxisView& v, int D, int layout, int b, int swap) {
   BlockGeom g;
   if (layout == LAYOUT_DENSE) {
@@ -79,9 +91,19 @@ __device__ __forceinline__ void stage_block(CT* Ms, const double2* mat, const Bl
   }
 }
 
+// A batch of nb independent circuits of one structure: grid.z indexes the
+// circuit; its state, matrix and partial sums sit at z times these strides
+// (elements of the state type, double2 entries, double2 entries).
+struct BatchArg {
+  int nb = 1;
+  int64_t state_stride = 0;
+  int64_t mat_stride = 0;
+  int64_t part_stride = 0;
+};
+
 // Apply a built matrix (FP64 in `mat`, layout LAYOUT_*) on a view: out = M in.
 int launch_apply(int dtype, const void* in, void* out, const AxisView& v, int D, int layout,
-                 const double2* mat, int mflags, cudaStream_t st);
+                 const double2* mat, int mflags, cudaStream_t st, const BatchArg& bt = BatchArg());
 
 // Adjoint step of one op: lam_in = M^dagger lam_out (skipped when lam_in is
 // null) and the per-CTA partial sums of
@@ -90,7 +112,7 @@ int launch_apply(int dtype, const void* in, void* out, const AxisView& v, int D,
 // adjoint_grid_x(...).  launch_reduce_partials sums them in a fixed order.
 int launch_adjoint_partials(int dtype, const void* psi_in, const void* lam_out, void* lam_in,
                             const AxisView& v, int D, int layout, const double2* mat, int mflags,
-                            double2* cpart, int gx, cudaStream_t st);
+                            double2* cpart, int gx, cudaStream_t st, const BatchArg& bt = BatchArg());
 int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* cout, cudaStream_t st);
 int64_t adjoint_scratch_entries(int dtype, const AxisView& v, int D, int layout);
 int adjoint_grid_x(int dtype, const AxisView& v, int D, int layout);

@@ -499,8 +499,10 @@ __device__ void run_build_job(const BuildJob& J, const PhaseTerm* terms, const d
 }
 
 __global__ void build_jobs_kernel(const BuildJob* jobs, const PhaseTerm* terms, const double* params,
-                                  double2* arena) {
-  run_build_job(jobs[blockIdx.x], terms, params, arena);
+                                  double2* arena, int64_t param_stride, int64_t arena_stride) {
+  // blockIdx.y: circuit of a batch (own parameters, own matrix arena)
+  run_build_job(jobs[blockIdx.x], terms, params ? params + blockIdx.y * param_stride : nullptr,
+                arena + blockIdx.y * arena_stride);
 }
 
 #define MAX_INLINE_TERMS 8
@@ -514,9 +516,11 @@ __global__ void build_inline_kernel(InlineBuild b, double2* arena) {
 }
 
 int launch_build_jobs(const BuildJob* d_jobs, int n_jobs, const PhaseTerm* d_terms,
-                      const double* d_params, double2* arena, cudaStream_t st) {
+                      const double* d_params, double2* arena, cudaStream_t st, int nb, int64_t param_stride,
+                      int64_t arena_stride) {
   if (n_jobs <= 0) return FOCK_OK;
-  build_jobs_kernel<<<n_jobs, 256, 0, st>>>(d_jobs, d_terms, d_params, arena);
+  build_jobs_kernel<<<dim3(n_jobs, nb), 256, 0, st>>>(d_jobs, d_terms, d_params, arena, param_stride,
+                                                      arena_stride);
   FOCK_LAUNCH_CHECK("build_jobs_kernel");
   return FOCK_OK;
 }
@@ -551,8 +555,12 @@ int build_single(int gate, int layout, int D, double p0, double p1, const PhaseT
 // ---------------------------------------------------------------------------
 __global__ void param_grads_kernel(const GradOp* ops, const GradContrib* contrib, const int* pstart,
                                    const int* plist, const double2* arena, const double2* carena,
-                                   double* grads) {
+                                   double* grads, int n_params, int64_t arena_stride, int64_t carena_stride) {
   const int p = blockIdx.x;
+  // blockIdx.y: circuit of a batch
+  arena += blockIdx.y * arena_stride;
+  carena += blockIdx.y * carena_stride;
+  grads += (int64_t)blockIdx.y * n_params;
   __shared__ double red[256];
   double total = 0.0;
   for (int q = pstart[p]; q < pstart[p + 1]; ++q) {
@@ -595,11 +603,11 @@ __global__ void param_grads_kernel(const GradOp* ops, const GradContrib* contrib
 int launch_param_grads(const GradOp* d_ops, const GradContrib* d_contrib, const int* d_pstart,
                        const int* d_plist, int n_params, const PhaseTerm* d_terms,
                        const double2* arena, const double2* carena, double* grads,
-                       cudaStream_t st) {
+                       cudaStream_t st, int nb, int64_t arena_stride, int64_t carena_stride) {
   (void)d_terms;
   if (n_params <= 0) return FOCK_OK;
-  param_grads_kernel<<<n_params, 256, 0, st>>>(d_ops, d_contrib, d_pstart, d_plist, arena, carena,
-                                               grads);
+  param_grads_kernel<<<dim3(n_params, nb), 256, 0, st>>>(d_ops, d_contrib, d_pstart, d_plist, arena, carena,
+                                                         grads, n_params, arena_stride, carena_stride);
   FOCK_LAUNCH_CHECK("param_grads_kernel");
   return FOCK_OK;
 }

@@ -75,8 +75,9 @@ int64_t layout_entries(int layout, int D);
 int64_t build_scratch_entries(int gate, int D);
 int gate_layout(int gate);
 int launch_build_jobs(const BuildJob* d_jobs, int n_jobs, const PhaseTerm* d_terms,
-                      const double* d_params, double2* arena, cudaStream_t st);
+                      const double* d_params, double2* arena, cudaStream_t st, int nb = 1,
+                      int64_t param_stride = 0, int64_t arena_stride = 0);
 int launch_param_grads(const GradOp* d_ops, const GradContrib* d_contrib, const int* d_pstart,
                        const int* d_plist, int n_params, const PhaseTerm* d_terms,
                        const double2* arena, const double2* carena, double* grads,
-                       cudaStream_t st);
+                       cudaStream_t st, int nb = 1, int64_t arena_stride = 0, int64_t carena_stride = 0);

@@ -49,6 +49,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct fock_plan {
   int N = 0, D = 0, pure = 1, dtype = 0, n_params = 0, n_gates = 0;
+  int batch = 1;  // circuits of this structure run together (grid.z)
   std::vector<PlanOp> ops;
   // table image (pinned host memory) and its sections
   unsigned char* host = nullptr;
@@ -79,9 +80,13 @@ static int ensure_events(std::vector<cudaEvent_t>& ev, size_t n) {
 // batched reduction of all ops' partial C sums
 // ---------------------------------------------------------------------------
 __global__ void reduce_all_kernel(const RedOp* __restrict__ ops, int n_ops, int64_t total,
-                                  const double2* __restrict__ cpart, double2* __restrict__ carena) {
+                                  const double2* __restrict__ cpart, double2* __restrict__ carena,
+                                  int64_t cpart_stride) {
   const int lane = threadIdx.x & 31;
-  const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  // blockIdx.y: circuit of a batch
+  cpart += blockIdx.y * cpart_stride;
+  carena += blockIdx.y * total;
   if (e >= total) return;
   int lo = 0, hi = n_ops - 1;
   while (lo < hi) {  // last op with c_off <= e
@@ -157,7 +162,13 @@ static void absorb_pending(PlanOp& op, int mode, std::vector<std::vector<Pending
 
 extern "C" int fock_plan_create(int num_modes, int cutoff, int pure, int dtype, const fock_gate* gates,
                                 int n_gates, int n_params, fock_plan** out) {
+  return fock_plan_create_batch(num_modes, cutoff, pure, dtype, gates, n_gates, n_params, 1, out);
+}
+
+extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int dtype, const fock_gate* gates,
+                                      int n_gates, int n_params, int batch, fock_plan** out) {
   if (!out) return fock_set_error(FOCK_ERR_INVALID, "null output pointer");
+  if (batch < 1 || batch > 65535) return fock_set_error(FOCK_ERR_INVALID, "batch must be in [1, 65535], got %d", batch);
   *out = nullptr;
   if (dtype != FOCK_C64 && dtype != FOCK_C128) return fock_set_error(FOCK_ERR_INVALID, "bad dtype");
   if (cutoff < 1 || cutoff > FOCK_MAX_CUTOFF) return fock_set_error(FOCK_ERR_INVALID, "bad cutoff %d", cutoff);
@@ -168,6 +179,7 @@ extern "C" int fock_plan_create(int num_modes, int cutoff, int pure, int dtype, 
   if (num_modes * log2((double)cutoff) > 60.0) return fock_set_error(FOCK_ERR_INVALID, "state too large");
 
   fock_plan* P = new fock_plan();
+  P->batch = batch;
   P->N = num_modes; P->D = cutoff; P->pure = pure; P->dtype = dtype; P->n_params = n_params;
   P->n_gates = n_gates;
   const int N = num_modes, D = cutoff;
@@ -343,9 +355,9 @@ extern "C" int fock_plan_create(int num_modes, int cutoff, int pure, int dtype, 
   P->o_plist = o; o = align256(o + sizeof(int) * std::max(n_contrib, 1));
   P->o_red = o; o = align256(o + sizeof(RedOp) * std::max(n_ops, 1));
   P->tables_bytes = o;
-  P->o_arena = o; o = align256(o + sizeof(double2) * arena);
-  P->o_carena = o; o = align256(o + sizeof(double2) * std::max<int64_t>(carena, 1));
-  P->o_cpart = o; o = align256(o + sizeof(double2) * std::max<int64_t>(cpart, 1));
+  P->o_arena = o; o = align256(o + sizeof(double2) * arena * batch);
+  P->o_carena = o; o = align256(o + sizeof(double2) * std::max<int64_t>(carena, 1) * batch);
+  P->o_cpart = o; o = align256(o + sizeof(double2) * std::max<int64_t>(cpart, 1) * batch);
   P->ws_bytes = o;
 
   if (cudaHostAlloc((void**)&P->host, P->tables_bytes, cudaHostAllocDefault) != cudaSuccess) {
@@ -426,8 +438,9 @@ extern "C" int fock_plan_get_info(const fock_plan* P, fock_plan_info* info) {
   info->state_elems = P->state_elems;
   info->state_bytes = P->state_elems * (P->dtype == FOCK_C64 ? 8 : 16);
   info->workspace_bytes = (int64_t)P->ws_bytes;
-  info->flops_fwd = P->flops_fwd;
-  info->bytes_fwd = 2 * info->state_bytes * (int64_t)P->ops.size();
+  info->flops_fwd = P->flops_fwd * P->batch;
+  info->bytes_fwd = 2 * info->state_bytes * (int64_t)P->ops.size() * P->batch;
+  info->batch = P->batch;
   return FOCK_OK;
 }
 
@@ -454,7 +467,7 @@ static int upload_and_build(fock_plan* P, const double* params, unsigned char* w
     // one table
   }
   return launch_build_jobs((const BuildJob*)(ws + P->o_jobs), n_ops, (const PhaseTerm*)(ws + P->o_terms),
-                           params, (double2*)(ws + P->o_arena), st);
+                           params, (double2*)(ws + P->o_arena), st, P->batch, P->n_params, P->arena_entries);
 }
 
 extern "C" int fock_plan_forward(fock_plan* P, const double* params, const void* state_in, void* states,
@@ -467,8 +480,12 @@ extern "C" int fock_plan_forward(fock_plan* P, const double* params, const void*
   int rc = upload_and_build(P, params, ws, 0, st);
   if (rc) return rc;
   const int esz = P->dtype == FOCK_C64 ? 8 : 16;
-  const int64_t sb = P->state_elems * esz;
+  const int64_t sb = P->state_elems * esz * P->batch;  // one op's states for the whole batch
   const double2* arena = (const double2*)(ws + P->o_arena);
+  BatchArg bt;
+  bt.nb = P->batch;
+  bt.state_stride = P->state_elems;
+  bt.mat_stride = P->arena_entries;
   const void* cur = state_in;
   const int n_ops = (int)P->ops.size();
   if (P->timing) {
@@ -479,7 +496,7 @@ extern "C" int fock_plan_forward(fock_plan* P, const double* params, const void*
     const PlanOp& op = P->ops[k];
     void* dst = (char*)states + (store_all ? (int64_t)k : (int64_t)(k & 1)) * sb;
     if (P->timing) FOCK_CUDA_TRY(cudaEventRecord(P->ev_fwd[k], st));
-    rc = launch_apply(P->dtype, cur, dst, op.view, P->D, op.layout, arena + op.m_off, op.swap ? MF_SWAP : 0, st);
+    rc = launch_apply(P->dtype, cur, dst, op.view, P->D, op.layout, arena + op.m_off, op.swap ? MF_SWAP : 0, st, bt);
     if (rc) return rc;
     cur = dst;
   }
@@ -502,9 +519,14 @@ extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void
   int rc = upload_and_build(P, params, ws, 1, st);
   if (rc) return rc;
   const int esz = P->dtype == FOCK_C64 ? 8 : 16;
-  const int64_t sb = P->state_elems * esz;
+  const int64_t sb = P->state_elems * esz * P->batch;
   const double2* arena = (const double2*)(ws + P->o_arena);
   double2* cpart = (double2*)(ws + P->o_cpart);
+  BatchArg bt;
+  bt.nb = P->batch;
+  bt.state_stride = P->state_elems;
+  bt.mat_stride = P->arena_entries;
+  bt.part_stride = P->cpart_entries;
   const int n_ops = (int)P->ops.size();
   void* lam = grad_state;
   void* other = grad_tmp;
@@ -517,7 +539,7 @@ extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void
     const void* psi_in = k == 0 ? state_in : (const char*)states + (int64_t)(k - 1) * sb;
     if (P->timing) FOCK_CUDA_TRY(cudaEventRecord(P->ev_bwd[k + 1], st));
     rc = launch_adjoint_partials(P->dtype, psi_in, lam, other, op.view, P->D, op.layout, arena + op.m_off,
-                                 op.swap ? MF_SWAP : 0, cpart + op.cpart_off, op.gx, st);
+                                 op.swap ? MF_SWAP : 0, cpart + op.cpart_off, op.gx, st, bt);
     if (rc) return rc;
     void* t = lam;
     lam = other;
@@ -530,15 +552,16 @@ extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void
   if (lam != grad_state) FOCK_CUDA_TRY(cudaMemcpyAsync(grad_state, lam, sb, cudaMemcpyDeviceToDevice, st));
   if (n_ops > 0) {
     const int64_t threads = P->carena_entries * 32;
-    reduce_all_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-        (const RedOp*)(ws + P->o_red), n_ops, P->carena_entries, cpart, (double2*)(ws + P->o_carena));
+    reduce_all_kernel<<<dim3((unsigned)((threads + 255) / 256), P->batch), 256, 0, st>>>(
+        (const RedOp*)(ws + P->o_red), n_ops, P->carena_entries, cpart, (double2*)(ws + P->o_carena),
+        P->cpart_entries);
     FOCK_LAUNCH_CHECK("reduce_all_kernel");
   }
   if (P->n_params > 0) {
     rc = launch_param_grads((const GradOp*)(ws + P->o_gops), (const GradContrib*)(ws + P->o_contrib),
                             (const int*)(ws + P->o_pstart), (const int*)(ws + P->o_plist), P->n_params,
                             (const PhaseTerm*)(ws + P->o_terms), arena, (const double2*)(ws + P->o_carena),
-                            grad_params, st);
+                            grad_params, st, P->batch, P->arena_entries, P->carena_entries);
     if (rc) return rc;
   }
   return FOCK_OK;

@@ -164,3 +164,31 @@ def test_known_gradient_displacement_mean_photon(cuda):
     (torch.sum(n * torch.abs(psi) ** 2)).backward()
     assert abs(p.grad[0].item() - 2 * r) < 1e-9
     assert abs(p.grad[1].item()) < 1e-12
+
+
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_batched_circuits_match_individual_runs(cuda, dtype):
+    """B circuits of one structure with their own parameters (TF batch axis)."""
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+    from strawberryfields_gb300.qnn import qnn_gates, qnn_params, target_state
+
+    N, D, B = 3, 6, 5
+    gates, npar = qnn_gates(N, 2)
+    P = np.stack([qnn_params(gates, npar, seed=20 + b) for b in range(B)])
+    tdt = torch.complex128 if dtype == "complex128" else torch.complex64
+    circ = CompiledCircuit(N, D, gates, npar, dtype=tdt, batch=B)
+    p = torch.tensor(P, device="cuda", requires_grad=True)
+    psi = circ(p)
+    assert tuple(psi.shape) == (B,) + (D,) * N
+    t = target_state(N, D, 3, seed=4)
+    tt = torch.as_tensor(t, device="cuda").to(tdt)
+    s = torch.sum(tt.conj() * psi, dim=tuple(range(1, N + 1)))
+    (1 - torch.abs(s) ** 2).sum().backward()
+    tol = 1e-12 if dtype == "complex128" else 1e-5
+    for b in range(B):
+        ref_states = fo.run_gates(gates, P[b], N, D)
+        assert np.abs(psi[b].detach().to(torch.complex128).cpu().numpy() - ref_states[-1]).max() < tol
+        ref = fo.adjoint_grads(gates, P[b], N, D, _loss_grad(ref_states[-1], t)[1])
+        rel = np.linalg.norm(p.grad[b].cpu().numpy() - ref) / np.linalg.norm(ref)
+        assert rel < (1e-10 if dtype == "complex128" else 1e-5), (b, rel)
