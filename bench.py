@@ -220,15 +220,30 @@ def gpu_arm(args, rank, world, cpu_base):
     for _ in range(args.warmup):
         step(p_dev)
     torch.cuda.synchronize()
+    lib = _lib.load()
+    # forward + loss + adjoint captured as one CUDA graph (no per-op events
+    # inside the timed graph)
+    from strawberryfields_gb300.autograd import GraphedGradient
+
+    def loss_fn(psi):
+        s = torch.sum(t.conj() * psi)
+        return 1 - (s.real ** 2 + s.imag ** 2)
+
+    def run(graphed):
+        if graphed is not None:
+            loss, g = graphed(p_dev)
+        else:
+            g, loss = step(p_dev)
+        return g
+
+    graphed = None
+    if not args.eager:
+        graphed = GraphedGradient(circ, loss_fn, p_dev, warmup=1)
+        for _ in range(args.warmup):
+            graphed(p_dev)
+        torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    lib = _lib.load()
-    _lib.check(lib.fock_plan_enable_timing(circ._plan, 1))
-    nops = circ.n_ops
-    fwd_ms = np.zeros(nops, dtype=np.float32)
-    bwd_ms = np.zeros(nops, dtype=np.float32)
-    fbuf = (ctypes.c_float * nops)()
-    bbuf = (ctypes.c_float * nops)()
     clocks = ClockSampler(dev.index)
     clocks.start()
     st = torch.cuda.current_stream(dev)
@@ -238,25 +253,40 @@ def gpu_arm(args, rank, world, cpu_base):
     for k in range(args.steps):
         flush.zero_()
         evs[k][0].record(st)
-        g, loss = step(p_dev)
+        run(graphed)
         evs[k][1].record(st)
-        evs[k][1].synchronize()
-        _lib.check(lib.fock_plan_op_times(circ._plan, fbuf, bbuf))
-        fwd_ms += np.frombuffer(fbuf, dtype=np.float32)
-        bwd_ms += np.frombuffer(bbuf, dtype=np.float32)
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
-    _lib.check(lib.fock_plan_enable_timing(circ._plan, 0))
     step_ms = [a.elapsed_time(b) for a, b in evs]
     from strawberryfields_gb300.replicas import job_throughput
 
     value, my_ms = job_throughput(float(np.sum(step_ms)), args.steps)
     ms_per_step = my_ms / args.steps
 
-    # per-op kernel roofline (averages over the timed steps)
-    fwd_ms /= args.steps
-    bwd_ms /= args.steps
+    # per-op kernel times: the same step with an event before and after every
+    # op (a separate capture, after the timed region)
+    _lib.check(lib.fock_plan_enable_timing(circ._plan, 1))
+    timed = GraphedGradient(circ, loss_fn, p_dev, warmup=1) if not args.eager else None
+    nops = circ.n_ops
+    fwd_ms = np.zeros(nops, dtype=np.float32)
+    bwd_ms = np.zeros(nops, dtype=np.float32)
+    fbuf = (ctypes.c_float * nops)()
+    bbuf = (ctypes.c_float * nops)()
+    op_steps = max(1, min(args.steps, 5))
+    for k in range(op_steps):
+        flush.zero_()
+        run(timed)
+        torch.cuda.synchronize()
+        _lib.check(lib.fock_plan_op_times(circ._plan, fbuf, bbuf))
+        fwd_ms += np.frombuffer(fbuf, dtype=np.float32)
+        bwd_ms += np.frombuffer(bbuf, dtype=np.float32)
+    _lib.check(lib.fock_plan_enable_timing(circ._plan, 0))
+    del timed
+
+    # per-op kernel roofline (averages over the op-timing steps)
+    fwd_ms /= op_steps
+    bwd_ms /= op_steps
     ops = circ.ops()
     S = circ.info.state_bytes
     peak, peak_kind = _peaks()
@@ -314,32 +344,38 @@ def gpu_arm(args, rank, world, cpu_base):
     p_host = torch.tensor(params).pin_memory()
     g_host = torch.empty(npar, dtype=torch.float64).pin_memory()
     l_host = torch.empty(1, dtype=torch.float32).pin_memory()
-    for _ in range(args.warmup):
+    def e2e_step():
         pd = p_host.to(dev, non_blocking=True)
-        g, loss = step(pd)
+        if graphed is not None:
+            loss, g = graphed(pd)
+        else:
+            g, loss = step(pd)
         g_host.copy_(g, non_blocking=True)
         l_host.copy_(loss.detach().reshape(1), non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
     torch.cuda.synchronize()
     e0.record(st)
     for _ in range(args.steps):
-        pd = p_host.to(dev, non_blocking=True)
-        g, loss = step(pd)
-        g_host.copy_(g, non_blocking=True)
-        l_host.copy_(loss.detach().reshape(1), non_blocking=True)
+        e2e_step()
     e1.record(st)
     e1.synchronize()
     e2e_ms = e0.elapsed_time(e1) / args.steps
     e2e = {"value": world * 1e3 / e2e_ms, "unit": "grads/s", "h2d_bytes_per_step": npar * 8,
            "d2h_bytes_per_step": npar * 8 + 4, "ms_per_step": e2e_ms}
 
-    launches = 2 * nops + 4
+    # ours per step: matrix build + nops applies (forward); matrix build +
+    # nops adjoints + nops partial-sum reductions + parameter gradients
+    launches = 3 * nops + 3
     out = {
         "metric": "CV-QNN grads/s (batched adjoint vs plain kernel+FD, <=1e-5 err); HBM % of peak",
         "value": round(value, 3), "unit": "grads/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 state / fp64 recurrences",
         "data": "synthetic seeded CV-QNN parameters and target",
-        "config": _config({"fused_ops": nops, "wall_s_timed": round(wall, 3)}),
+        "config": _config({"fused_ops": nops, "wall_s_timed": round(wall, 3),
+                           "execution": "eager" if graphed is None else "one CUDA graph per step"}),
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "kernels": kern,
         "grad_rel_err_vs_fp64": grad_err,
         "fd_baseline": {"gpu_forward_ms": 1e3 * fwd_s, "grads_per_s": fd_grads_per_s,
@@ -353,16 +389,24 @@ def single_gate_case(args):
     """Single-gate kernels on a 7-mode cutoff-12 complex64 ket (287 MB, larger
     than L2): forward apply and adjoint of a squeezer on an inner axis and on
     the last axis, and of a beamsplitter on an inner and on the last adjacent
-    pair.  Each op is its own compiled one-gate circuit; bytes per launch are
-    2 S (apply) and 3 S (adjoint)."""
+    pair.  Each op is its own compiled one-gate circuit, timed with the plan's
+    per-op events (apply = the apply launch; adjoint = the adjoint launch and
+    its partial-sum reduction; the matrix build is outside both).  Bytes per
+    launch are 2 S (apply) and 3 S (adjoint); L2 is flushed before each."""
+    import ctypes
+
     import torch
 
     from strawberryfields_gb300 import CompiledCircuit
+    from strawberryfields_gb300 import _lib
 
     dev = torch.device("cuda", 0)
+    lib = _lib.load()
     N, D = 7, 12
     cases = {"dense1_inner": [(4, 2, -1, 0)], "dense1_last": [(4, 6, -1, 0)],
              "block2_inner": [(5, 2, 3, 0)], "block2_last": [(5, 5, 6, 0)]}
+    if args.only:
+        cases = {k: v for k, v in cases.items() if k in args.only.split(",")}
     rng = np.random.default_rng(0)
     x = torch.as_tensor(rng.normal(size=(D,) * N).astype(np.float32)
                         + 1j * rng.normal(size=(D,) * N).astype(np.float32), device=dev)
@@ -371,10 +415,11 @@ def single_gate_case(args):
     peak, peak_kind = _peaks()
     S = x.numel() * 8
     res = {}
-    st = torch.cuda.current_stream(dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    fbuf, bbuf = (ctypes.c_float * 1)(), (ctypes.c_float * 1)()
     for name, gates in cases.items():
         circ = CompiledCircuit(N, D, gates, 2, dtype=torch.complex64, device=dev)
+        _lib.check(lib.fock_plan_enable_timing(circ._plan, 1))
         p = torch.tensor([0.3, 0.7], device=dev, dtype=torch.float64)
         for _ in range(args.warmup):
             states = circ.forward_states(p, state_in=x)
@@ -382,18 +427,13 @@ def single_gate_case(args):
         ta, tb = [], []
         for _ in range(args.steps):
             flush.zero_()
-            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-            e0.record(st)
             states = circ.forward_states(p, state_in=x)
-            e1.record(st)
             flush.zero_()
-            e3 = torch.cuda.Event(enable_timing=True)
-            e3.record(st)
             circ.backward(p, states, lam, state_in=x)
-            e2.record(st)
-            e2.synchronize()
-            ta.append(e0.elapsed_time(e1))
-            tb.append(e3.elapsed_time(e2))
+            torch.cuda.synchronize(dev)
+            _lib.check(lib.fock_plan_op_times(circ._plan, fbuf, bbuf))
+            ta.append(fbuf[0])
+            tb.append(bbuf[0])
         ta_ms, tb_ms = float(np.median(ta)), float(np.median(tb))
         res[name] = {"apply_us": 1e3 * ta_ms, "apply_gbs": 2 * S / (ta_ms / 1e3) / 1e9,
                      "adjoint_us": 1e3 * tb_ms, "adjoint_gbs": 3 * S / (tb_ms / 1e3) / 1e9}
@@ -401,9 +441,58 @@ def single_gate_case(args):
             res[name][k.replace("gbs", "frac")] = res[name][k] / peak
         del circ, states
     print(json.dumps({"case": "single-gate", "state": f"{D}^{N} complex64 ({S / 1e6:.0f} MB)",
-                      "note": "apply = build + 1 apply launch; adjoint = build + 1 adjoint launch + reduce + "
-                              "param-grad launches (event span)",
+                      "note": "kernel time from per-op events: apply = 1 apply launch; adjoint = 1 adjoint "
+                              "launch + its partial-sum reduction (median over steps, L2 flushed before each)",
+                      "kernels_env": os.environ.get("FOCK_GB300_KERNELS", "default"),
                       "peak_gbs": peak, "peak_source": peak_kind, "kernels": res}))
+    return 0
+
+
+def batched_case(args):
+    """4096 independent CV-QNN circuits, modes U{2..5}, cutoff U{6..20}, depth
+    U{2..10} layers (seed 0), complex64: loss and full gradient of every
+    circuit per step.  Circuits are grouped by structure into batched compiled
+    circuits spread over CUDA streams; groups whose stored states would exceed
+    8 GB keep checkpoints."""
+    import torch
+
+    from strawberryfields_gb300.batch import CircuitBatch, random_qnn_batch
+    from strawberryfields_gb300.qnn import target_state
+
+    dev = torch.device("cuda", 0)
+    n = args.circuits
+    t0 = time.perf_counter()
+    circuits, params = random_qnn_batch(n, seed=0)
+    cb = CircuitBatch(circuits, dtype=torch.complex64, device=dev, streams=8)
+    setup_s = time.perf_counter() - t0
+    targets = {}
+    for nm, D, _, _ in circuits:
+        if (nm, D) not in targets:
+            targets[(nm, D)] = torch.as_tensor(target_state(nm, D, 6, seed=nm * 100 + D), device=dev)
+    pt = [torch.tensor(p, device=dev) for p in params]
+    for _ in range(args.warmup):
+        cb.value_and_grad(pt, targets)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        losses, grads = cb.value_and_grad(pt, targets)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    stats = cb.stats()
+    npar = int(sum(c[3] for c in circuits))
+    out = {"case": "batched", "metric": "circuits/s (forward + adjoint gradient of every circuit)",
+           "value": n / (ms / 1e3), "unit": "circuits/s", "ms_per_step": ms, "steps": args.steps,
+           "warmup": args.warmup, "grads_per_s": n / (ms / 1e3), "params_per_step": npar,
+           "config": {"workload": "4096 heterogeneous CV-QNN circuits", "circuits": n, "modes": "U{2..5}",
+                      "cutoff": "U{6..20}", "depth": "U{2..10} layers", "seed": 0, "dtype": "complex64"},
+           "groups": stats["groups"], "fused_ops": stats["ops"],
+           "algorithmic_tb_per_step": (stats["bytes_forward"] + stats["bytes_adjoint"]) / 1e12,
+           "achieved_gbs": (stats["bytes_forward"] + stats["bytes_adjoint"]) / (ms / 1e3) / 1e9,
+           "setup_s": setup_s}
+    print(json.dumps(out))
     return 0
 
 
@@ -414,10 +503,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--case", default="gradient", choices=["gradient", "single-gate"])
+    ap.add_argument("--case", default="gradient", choices=["gradient", "single-gate", "batched"])
+    ap.add_argument("--circuits", type=int, default=4096)
+    ap.add_argument("--only", default="", help="single-gate case: comma-separated subset of the kernels")
+    ap.add_argument("--eager", action="store_true", help="no CUDA graph capture")
     args = ap.parse_args()
     if args.case == "single-gate":
         return single_gate_case(args)
+    if args.case == "batched":
+        return batched_case(args)
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
 

@@ -155,13 +155,21 @@ int fock_reduced_dm1_noalloc(int num_modes, int cutoff, int pure, int dtype, int
 /* ---------------------------------------------- compiled circuits + adjoint (A1-A3)
  * A plan is a gate list compiled on the host: rotation/Kerr/cross-Kerr gates
  * are fused into the neighbouring non-diagonal gate, so the state crosses HBM
- * once per remaining op.  Forward: states[k] = op_k(states[k-1]) for the
- * n_ops fused ops (states[-1] = `state_in`); with store_all = 0 only two
- * slots are used (ping-pong).  Backward: the adjoint sweep of the gradient
- * contract of strawberryfields/backends/tfbackend/ops.py:190-454 (custom
- * gradients) and :688-854 (state contractions): given grad_state = dL/dpsi of
- * the final state (torch convention dL/dRe + i dL/dIm), accumulate dL/dparams
- * (device doubles, zeroed by the call) and leave dL/dpsi_in in grad_state. */
+ * once per remaining op.
+ * Forward: op k maps the previous state to its output; `store_every` = k
+ * decides which outputs are kept in `states` (slots of batch * D^n entries):
+ * 0 -> two ping-pong slots (final state in slot (n_ops-1) & 1); 1 -> every
+ * output (slot j, n_ops slots); k > 1 -> checkpoints: the output of op j goes
+ * to slot (j+1)/k - 1 when (j+1) % k == 0, the last op's output to slot
+ * ceil(n_ops/k) - 1, the rest through two scratch slots after them
+ * (ceil(n_ops/k) + 2 slots).
+ * Backward: the adjoint sweep of the gradient contract of
+ * strawberryfields/backends/tfbackend/ops.py:190-454 (custom gradients) and
+ * :688-854 (state contractions): given grad_state = dL/dpsi of the final state
+ * (torch convention dL/dRe + i dL/dIm), write dL/dparams and leave dL/dpsi_in
+ * in grad_state.  With store_every = k > 1 each segment of k ops is first
+ * recomputed from its checkpoint into `seg` (k - 1 slots), so memory is
+ * ceil(n_ops/k) + k + 1 states instead of n_ops. */
 typedef struct fock_plan fock_plan;
 typedef struct fock_plan_info {
   int32_t n_ops;            /* fused ops */
@@ -188,10 +196,10 @@ int fock_plan_get_info(const fock_plan* plan, fock_plan_info* info);
  * number-difference block), modes, number of gates fused into it. */
 int fock_plan_op(const fock_plan* plan, int k, int* kind, int* mode1, int* mode2, int* n_fused);
 int fock_plan_forward(fock_plan* plan, const double* params, const void* state_in, void* states,
-                      int store_all, void* workspace, void* stream);
+                      int store_every, void* workspace, void* stream);
 int fock_plan_backward(fock_plan* plan, const double* params, const void* state_in,
-                       const void* states, void* grad_state, void* grad_tmp, double* grad_params,
-                       void* workspace, void* stream);
+                       const void* states, int store_every, void* seg, void* grad_state, void* grad_tmp,
+                       double* grad_params, void* workspace, void* stream);
 
 /* Per-op device timing of plan sweeps (CUDA events recorded between the op
  * launches on the sweep's stream).  After enabling, every forward/backward

@@ -40,9 +40,14 @@ class CompiledCircuit:
             with its own parameters (parameters ``[batch, n_params]``, states
             ``[batch, D, ..., D]``) -- the batch axis of the reference's TF
             backend (``tfbackend/circuit.py:129-185``); 1 gives unbatched shapes
+        checkpoint (int): keep every ``checkpoint``-th op output for the
+            adjoint sweep and recompute the others segment by segment (1 keeps
+            all outputs; larger values trade one extra forward for
+            ``n_ops / checkpoint + checkpoint`` resident states instead of ``n_ops``)
     """
 
-    def __init__(self, num_modes, cutoff, gates, n_params, dtype=torch.complex64, device=None, batch=1):
+    def __init__(self, num_modes, cutoff, gates, n_params, dtype=torch.complex64, device=None, batch=1,
+                 checkpoint=1):
         lib = L.load()
         self.num_modes = int(num_modes)
         self.cutoff = int(cutoff)
@@ -55,6 +60,9 @@ class CompiledCircuit:
             arr[i].kind, arr[i].mode1, arr[i].mode2, arr[i].pidx = int(kind), int(m1), int(m2), int(pidx)
         plan = ctypes.c_void_p()
         self.batch = int(batch)
+        self.checkpoint = int(checkpoint)
+        if self.checkpoint < 1:
+            raise ValueError("checkpoint must be >= 1")
         L.check(lib.fock_plan_create_batch(self.num_modes, self.cutoff, 1, self._dcode, arr, len(gates),
                                            self.n_params, self.batch, ctypes.byref(plan)), "fock_plan_create")
         self._plan = plan
@@ -64,7 +72,7 @@ class CompiledCircuit:
         self.n_gates = len(gates)
         self.shape = [self.cutoff] * self.num_modes
         self._bshape = ([self.batch] if self.batch > 1 else []) + self.shape
-        self._ws = torch.empty(int(info.workspace_bytes), dtype=torch.uint8, device=self.device)
+        self._ws_buf = None
         self._vacuum = torch.zeros([self.batch, int(info.state_elems)], dtype=self.dtype, device=self.device)
         self._vacuum[:, 0] = 1.0
         self._vacuum = self._vacuum.reshape(self._bshape)
@@ -77,6 +85,17 @@ class CompiledCircuit:
             except Exception:  # interpreter shutdown
                 pass
             self._plan = None
+
+    @property
+    def _ws(self):
+        """Workspace (allocated on first use; ``release()`` returns it)."""
+        if self._ws_buf is None:
+            self._ws_buf = torch.empty(int(self.info.workspace_bytes), dtype=torch.uint8, device=self.device)
+        return self._ws_buf
+
+    def release(self):
+        """Drop the workspace until the next sweep (memory reuse across plans)."""
+        self._ws_buf = None
 
     @property
     def n_ops(self):
@@ -104,23 +123,41 @@ class CompiledCircuit:
             raise ValueError(f"expected {self.batch} x {self.n_params} parameters, got {tuple(p.shape)}")
         return p.contiguous()
 
-    def forward_states(self, params, state_in=None, store_all=True):
-        """Run the forward sweep; returns the [n_ops, D..] tensor of op outputs
-        (the last one is the final state).  With store_all=False only two
-        slots are kept and the final state is returned alone."""
+    def _slots(self, k):
+        n = self.n_ops
+        if k <= 0:
+            return 2
+        if k == 1:
+            return n
+        return -(-n // k) + 2
+
+    def final_index(self, k=None):
+        """Slot of the final state in a forward sweep with store_every = k."""
+        k = self.checkpoint if k is None else k
+        n = self.n_ops
+        if k <= 0:
+            return (n - 1) & 1
+        if k == 1:
+            return n - 1
+        return -(-n // k) - 1
+
+    def forward_states(self, params, state_in=None, store_all=True, store_every=None):
+        """Run the forward sweep and return the kept states ([slots, ...]):
+        every op output (``store_every=1``), checkpoints (``> 1``), or, with
+        ``store_all=False``, only the final state."""
         p = self._params(params)
         x = self._vacuum if state_in is None else state_in.to(self.dtype).contiguous()
         n = self.n_ops
         if n == 0:
             return x.clone().unsqueeze(0)
-        slots = n if store_all else min(n, 2)
-        states = torch.empty([slots] + self._bshape, dtype=self.dtype, device=self.device)
+        k = (self.checkpoint if store_every is None else int(store_every)) if store_all else 0
+        states = torch.empty([self._slots(k)] + self._bshape, dtype=self.dtype, device=self.device)
         L.check(L.load().fock_plan_forward(self._plan, p.data_ptr(), x.data_ptr(), states.data_ptr(),
-                                           int(store_all), self._ws.data_ptr(), self._stream()),
+                                           k, self._ws.data_ptr(), self._stream()),
                 "fock_plan_forward")
-        if store_all:
-            return states
-        return states[(n - 1) & 1]
+        if not store_all:
+            return states[self.final_index(0)]
+        return states
 
     def backward(self, params, states, grad_state, state_in=None):
         """Adjoint sweep: returns (dL/dparams, dL/dstate_in) given dL/dpsi_final."""
@@ -133,9 +170,12 @@ class CompiledCircuit:
         if self.n_ops == 0:
             grads.zero_()
             return grads, lam
-        L.check(L.load().fock_plan_backward(self._plan, p.data_ptr(), x.data_ptr(), states.data_ptr(),
-                                            lam.data_ptr(), tmp.data_ptr(), grads.data_ptr(),
-                                            self._ws.data_ptr(), self._stream()),
+        k = self.checkpoint
+        seg = torch.empty([max(k - 1, 1)] + self._bshape, dtype=self.dtype, device=self.device) if k > 1 else None
+        L.check(L.load().fock_plan_backward(self._plan, p.data_ptr(), x.data_ptr(), states.data_ptr(), k,
+                                            seg.data_ptr() if seg is not None else None, lam.data_ptr(),
+                                            tmp.data_ptr(), grads.data_ptr(), self._ws.data_ptr(),
+                                            self._stream()),
                 "fock_plan_backward")
         return grads, lam
 
@@ -151,7 +191,7 @@ class _CircuitFunction(torch.autograd.Function):
         ctx.circ = circ
         ctx.state_in = state_in
         ctx.save_for_backward(params.detach(), states)
-        return states[-1].clone() if circ.n_ops else states[0]
+        return states[circ.final_index()].clone() if circ.n_ops else states[0]
 
     @staticmethod
     def backward(ctx, grad_out):
@@ -159,3 +199,48 @@ class _CircuitFunction(torch.autograd.Function):
         grads, lam = ctx.circ.backward(params, states, grad_out, ctx.state_in)
         gin = lam if (ctx.state_in is not None and ctx.needs_input_grad[2]) else None
         return grads.to(params.dtype), None, gin
+
+
+class GraphedGradient:
+    """One gradient step -- fused forward sweep, the loss, the adjoint sweep --
+    captured once as a CUDA graph and replayed (the spec design: the
+    whole forward+backward as one graph launch, no per-kernel host work).
+
+    Args:
+        circ (CompiledCircuit): the circuit
+        loss_fn (callable): maps the final state tensor to a scalar loss
+            (torch ops only: no host synchronisation inside)
+        params (torch.Tensor): example parameters (shape and device)
+        warmup (int): eager steps on a side stream before capture
+    """
+
+    def __init__(self, circ, loss_fn, params, warmup=2):
+        self.circ = circ
+        self.loss_fn = loss_fn
+        self.static_p = torch.as_tensor(params).detach().to(device=circ.device, dtype=torch.float64).clone()
+        cur = torch.cuda.current_stream(circ.device)
+        side = torch.cuda.Stream(device=circ.device)
+        side.wait_stream(cur)
+        with torch.cuda.stream(side):
+            for _ in range(warmup):
+                self._step()
+        cur.wait_stream(side)
+        torch.cuda.synchronize(circ.device)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.static_loss, self.static_grad = self._step()
+
+    def _step(self):
+        p = self.static_p.detach().requires_grad_(True)
+        psi = self.circ(p)
+        loss = self.loss_fn(psi)
+        (g,) = torch.autograd.grad(loss, p)
+        return loss.detach(), g
+
+    def __call__(self, params=None):
+        """Replay with new parameters (copied into the captured buffer);
+        returns (loss, gradient) tensors owned by the graph."""
+        if params is not None:
+            self.static_p.copy_(params, non_blocking=True)
+        self.graph.replay()
+        return self.static_loss, self.static_grad

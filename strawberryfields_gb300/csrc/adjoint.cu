@@ -15,42 +15,37 @@
 // the CTA forms the s x s outer-product sum C over the tile as a small
 // register-tiled GEMM: 16 owners hold an RR x RR sub-block each (RR =
 // ceil(s/4)), NG = TILE/16 groups split the tile's columns, so every shared
-// load feeds RR complex FMAs.  The loads of the CTA's next tile are issued
-// before the contraction of the current one, so they are in flight while it
-// runs.  Grid: about 8 CTAs per SM over all blocks, largest blocks first;
-// kernels are compiled per cutoff bucket so registers match the block size.
+// load feeds RR complex FMAs.  Tiles arrive in shared memory through
+// cp.async (no register staging), which keeps registers low enough for three
+// resident CTAs per SM.  Grid: about 8 CTAs per SM over all blocks, largest
+// blocks first; kernels are compiled per cutoff bucket.
 // Partial C's of each CTA go to `cpart` ([gridDim.x][entries], FP64); a
 // separate deterministic reduction sums them.
 #include "apply.cuh"
 
+#include <string.h>
+
 template <int S> struct RRof { static const int value = (S + 3) / 4; };
 
-// Loads of one column of lam_out and psi_in (S values each) into registers.
-template <typename CT, int S>
-__device__ __forceinline__ void adj_load(const CT* __restrict__ psi_in, const CT* __restrict__ lam_out,
-                                         const AxisView& v, int D, const BlockGeom& g, int64_t j, CT* lam,
-                                         CT* psi) {
-  if (j < v.ncols) {
-    const int64_t base = col_base(v, j, D) + g.boff;
-#pragma unroll
-    for (int u = 0; u < S; ++u) {
-      lam[u] = __ldg(lam_out + base + u * g.step);
-      psi[u] = __ldg(psi_in + base + u * g.step);
-    }
-  } else {
-#pragma unroll
-    for (int u = 0; u < S; ++u) {
-      lam[u] = czero<CT>();
-      psi[u] = czero<CT>();
-    }
-  }
+// Asynchronous global -> shared copies (cp.async): the tile lands in shared
+// memory without passing through registers; invalid columns are zero-filled.
+__device__ __forceinline__ void cp_async_elem(float2* dst, const float2* src, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(src), "r"(valid ? 8 : 0));
 }
+__device__ __forceinline__ void cp_async_elem(double2* dst, const double2* src, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(src), "r"(valid ? 16 : 0));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 template <typename CT, int S, int TILE>
 __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, const CT* __restrict__ lam_out,
-                                             CT* __restrict__ lam_in, const AxisView& v, int D,
-                                             const CT* MsH, CT* lam_s, CT* psi_s, const BlockGeom& g,
-                                             double2* __restrict__ cpart, int64_t nent, int write_lam) {
+                                             CT* __restrict__ lam_in, const AxisView& v, int D, CT* MsH,
+                                             const double2* __restrict__ mat, int mflags, CT* lam_s, CT* psi_s,
+                                             const BlockGeom& g, double2* __restrict__ mypart, int xrank, int gxb,
+                                             int write_lam) {
   constexpr int RR = RRof<S>::value;
   constexpr int NG = TILE / 16;
   constexpr int LD = TILE + 1;  // padded row stride (elements)
@@ -64,18 +59,36 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
     for (int c = 0; c < RR; ++c) acc[r][c] = czero<CT>();
 
   const int64_t ntiles = (v.ncols + TILE - 1) / TILE;
-  CT lam[S], psi[S];
-  int64_t t = blockIdx.x;
-  if (t < ntiles) adj_load<CT, S>(psi_in, lam_out, v, D, g, t * TILE + tid, lam, psi);
-  for (; t < ntiles; t += gridDim.x) {
+  auto issue = [&](int64_t t) {
     const int64_t j = t * TILE + tid;
+    const bool valid = j < v.ncols;
+    const int64_t base = valid ? col_base(v, j, D) + g.boff : 0;
 #pragma unroll
     for (int u = 0; u < S; ++u) {
-      lam_s[u * LD + tid] = lam[u];
-      psi_s[u * LD + tid] = psi[u];
+      const int64_t off = valid ? base + u * g.step : 0;
+      cp_async_elem(&lam_s[u * LD + tid], lam_out + off, valid);
+      cp_async_elem(&psi_s[u * LD + tid], psi_in + off, valid);
     }
+    cp_async_commit();
+  };
+  // the first tile's copies are in flight while the block is staged
+  if (xrank < ntiles) issue(xrank);
+  if (write_lam) stage_block(MsH, mat, g, mflags | MF_ADJOINT);
+  // padding rows s..4*RR-1 stay zero
+  for (int e = tid; e < (4 * RR - S) * LD; e += TILE) {
+    lam_s[S * LD + e] = czero<CT>();
+    psi_s[S * LD + e] = czero<CT>();
+  }
+  __syncthreads();
+  for (int64_t t = xrank; t < ntiles; t += gxb) {
+    cp_async_wait_all();  // this thread's column has landed
+    const int64_t j = t * TILE + tid;
     if (write_lam && j < v.ncols) {
+      // each thread reads back only its own column: no barrier needed here
       const int64_t base = col_base(v, j, D) + g.boff;
+      CT lam[S];
+#pragma unroll
+      for (int u = 0; u < S; ++u) lam[u] = lam_s[u * LD + tid];
 #pragma unroll
       for (int w = 0; w < S; ++w) {
         CT a = czero<CT>();
@@ -84,11 +97,8 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
         lam_in[base + w * g.step] = a;
       }
     }
-    __syncthreads();
-    // next tile's loads are in flight while this tile's contraction runs
-    const int64_t tn = t + gridDim.x;
-    if (tn < ntiles) adj_load<CT, S>(psi_in, lam_out, v, D, g, tn * TILE + tid, lam, psi);
-#pragma unroll 4
+    __syncthreads();  // every thread's column of tile t has landed
+#pragma unroll 2
     for (int step = 0; step < TILE / NG; ++step) {
       const int col = step * NG + grp;
       CT lv[RR], pv[RR];
@@ -101,7 +111,8 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
 #pragma unroll
         for (int c = 0; c < RR; ++c) cfma_conj(acc[r][c], lv[r], pv[c]);
     }
-    __syncthreads();
+    __syncthreads();  // the tile buffers are free for the next tile
+    if (t + gxb < ntiles) issue(t + gxb);
   }
   // reduce over the NG groups of each owner (adjacent lanes)
 #pragma unroll
@@ -115,7 +126,6 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
       }
   }
   if (grp == 0) {
-    double2* dst = cpart + (int64_t)blockIdx.x * nent + g.moff;
 #pragma unroll
     for (int r = 0; r < RR; ++r)
 #pragma unroll
@@ -124,7 +134,7 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
         if (u < S && w < S) {
           int a = g.rev ? S - 1 - u : u;
           int b = g.rev ? S - 1 - w : w;
-          dst[a * S + b] = to_d(acc[r][c]);
+          mypart[a * S + b] = to_d(acc[r][c]);
         }
       }
   }
@@ -132,14 +142,16 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
 
 template <typename CT, int TILE>
 __device__ void adjoint_generic(const CT* __restrict__ psi_in, const CT* __restrict__ lam_out,
-                                CT* __restrict__ lam_in, const AxisView& v, int D, const CT* MsH,
-                                const BlockGeom& g, double2* __restrict__ cpart, int64_t nent,
-                                int write_lam) {
+                                CT* __restrict__ lam_in, const AxisView& v, int D, CT* MsH,
+                                const double2* __restrict__ mat, int mflags, const BlockGeom& g,
+                                double2* __restrict__ mypart, int xrank, int gxb, int write_lam) {
+  if (write_lam) stage_block(MsH, mat, g, mflags | MF_ADJOINT);
+  __syncthreads();
   // large blocks (beyond the unrolled buckets): thread per C entry over this
   // CTA's share of the columns, then lam_in per column
   const int S = g.s;
-  const int64_t per = (v.ncols + gridDim.x - 1) / gridDim.x;
-  int64_t j0 = blockIdx.x * per, j1 = j0 + per;
+  const int64_t per = (v.ncols + gxb - 1) / gxb;
+  int64_t j0 = xrank * per, j1 = j0 + per;
   if (j1 > v.ncols) j1 = v.ncols;
   for (int e = threadIdx.x; e < S * S; e += blockDim.x) {
     int u = e / S, w = e - u * S;
@@ -150,7 +162,7 @@ __device__ void adjoint_generic(const CT* __restrict__ psi_in, const CT* __restr
       cfma_conj(a, ld, pd);
     }
     int aa = g.rev ? S - 1 - u : u, bb = g.rev ? S - 1 - w : w;
-    cpart[(int64_t)blockIdx.x * nent + g.moff + aa * S + bb] = a;
+    mypart[aa * S + bb] = a;
   }
   if (!write_lam) return;
   for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
@@ -166,49 +178,60 @@ __device__ void adjoint_generic(const CT* __restrict__ psi_in, const CT* __restr
 template <typename CT, int S, int DMAX, int TILE>
 struct AdjDispatch {
   __device__ __forceinline__ static void run(const CT* psi_in, const CT* lam_out, CT* lam_in, const AxisView& v,
-                                             int D, const CT* MsH, CT* lam_s, CT* psi_s, const BlockGeom& g,
-                                             double2* cpart, int64_t nent, int write_lam) {
-    if (g.s == S) adjoint_body<CT, S, TILE>(psi_in, lam_out, lam_in, v, D, MsH, lam_s, psi_s, g, cpart, nent, write_lam);
-    else AdjDispatch<CT, S + 1, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, lam_s, psi_s, g, cpart, nent, write_lam);
+                                             int D, CT* MsH, const double2* mat, int mflags, CT* lam_s, CT* psi_s,
+                                             const BlockGeom& g, double2* mypart, int xrank, int gxb,
+                                             int write_lam) {
+    if (g.s == S)
+      adjoint_body<CT, S, TILE>(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s, g, mypart, xrank,
+                                gxb, write_lam);
+    else
+      AdjDispatch<CT, S + 1, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s, g,
+                                              mypart, xrank, gxb, write_lam);
   }
 };
 template <typename CT, int DMAX, int TILE>
 struct AdjDispatch<CT, DMAX + 1, DMAX, TILE> {
   __device__ __forceinline__ static void run(const CT* psi_in, const CT* lam_out, CT* lam_in, const AxisView& v,
-                                             int D, const CT* MsH, CT*, CT*, const BlockGeom& g,
-                                             double2* cpart, int64_t nent, int write_lam) {
-    adjoint_generic<CT, TILE>(psi_in, lam_out, lam_in, v, D, MsH, g, cpart, nent, write_lam);
+                                             int D, CT* MsH, const double2* mat, int mflags, CT*, CT*,
+                                             const BlockGeom& g, double2* mypart, int xrank, int gxb,
+                                             int write_lam) {
+    adjoint_generic<CT, TILE>(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, g, mypart, xrank, gxb, write_lam);
   }
 };
 
+// 3 resident CTAs (24 warps) per SM for complex64 cutoffs up to 12
+template <typename CT, int DMAX> struct AdjMinBlocks {
+  static const int value = (sizeof(CT) == 8 && DMAX > 0 && DMAX <= 12) ? 3 : 1;
+};
+
 template <typename CT, int TILE, int DMAX>
-__global__ void __launch_bounds__(TILE) adjoint_block_kernel(const CT* __restrict__ psi_in,
-                                                             const CT* __restrict__ lam_out,
-                                                             CT* __restrict__ lam_in, AxisView v, int D,
-                                                             int layout, const double2* __restrict__ mat,
-                                                             int mflags, double2* __restrict__ cpart,
-                                                             int64_t nent, int write_lam, BatchArg bt) {
+__global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)
+    adjoint_block_kernel(const CT* __restrict__ psi_in, const CT* __restrict__ lam_out, CT* __restrict__ lam_in,
+                         AxisView v, int D, int layout, const double2* __restrict__ mat, int mflags,
+                         double2* __restrict__ cpart, AdjSched sc, int write_lam, BatchArg bt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // which block this CTA serves, and its rank x among that block's CTAs
+  int y = 0;
+  while (y + 1 < sc.nblk && (int)blockIdx.x >= sc.start[y + 1]) ++y;
+  const int xrank = (int)blockIdx.x - sc.start[y];
+  const int gxb = sc.gx[y];
   psi_in += blockIdx.z * bt.state_stride;
   lam_out += blockIdx.z * bt.state_stride;
   if (write_lam) lam_in += blockIdx.z * bt.state_stride;
   mat += blockIdx.z * bt.mat_stride;
   cpart += blockIdx.z * bt.part_stride;
-  const int b = layout == LAYOUT_DENSE ? 0 : block_of_y(D, blockIdx.y);
+  const int b = layout == LAYOUT_DENSE ? 0 : block_of_y(D, y);
   const BlockGeom g = block_geom(v, D, layout, b, (mflags & MF_SWAP) ? 1 : 0);
   const int s = g.s;
   const int rows = 4 * ((s + 3) / 4);
+  // partial slot of this CTA (stored-orientation block)
+  const int bs = layout == LAYOUT_DENSE ? 0 : ((layout == LAYOUT_DIFF && (mflags & MF_SWAP)) ? 2 * D - 2 - b : b);
+  double2* mypart = cpart + sc.part_off[bs] + (int64_t)xrank * s * s;
   CT* MsH = reinterpret_cast<CT*>(smem_raw);
-  CT* lam_s = MsH + s * s;
+  CT* lam_s = MsH + ((s * s + 1) & ~1);
   CT* psi_s = lam_s + rows * (TILE + 1);
-  if (write_lam) stage_block(MsH, mat, g, mflags | MF_ADJOINT);
-  // zero the padding rows once (rows s..rows-1 stay zero)
-  for (int e = threadIdx.x; e < (rows - s) * (TILE + 1); e += blockDim.x) {
-    lam_s[s * (TILE + 1) + e] = czero<CT>();
-    psi_s[s * (TILE + 1) + e] = czero<CT>();
-  }
-  __syncthreads();
-  AdjDispatch<CT, 1, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, lam_s, psi_s, g, cpart, nent, write_lam);
+  AdjDispatch<CT, 1, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s, g, mypart,
+                                      xrank, gxb, write_lam);
 }
 
 static int tile_of(int dtype) { return dtype == FOCK_C64 ? 256 : 128; }
@@ -216,67 +239,178 @@ static int tile_of(int dtype) { return dtype == FOCK_C64 ? 256 : 128; }
 static size_t adjoint_smem(int dtype, int D) {
   const int esz = dtype == FOCK_C64 ? 8 : 16;
   const int rows = 4 * ((D + 3) / 4);
-  return (size_t)esz * ((size_t)D * D + 2 * (size_t)rows * (tile_of(dtype) + 1));
+  // matrix + the lam and psi tiles
+  return (size_t)esz * ((size_t)((D * D + 1) & ~1) + 2 * (size_t)rows * (tile_of(dtype) + 1));
 }
 
-int adjoint_grid_x(int dtype, const AxisView& v, int D, int layout) {
-  const int nblk = layout == LAYOUT_DENSE ? 1 : 2 * D - 1;
+template <typename CT, int TILE, int DMAX>
+static int resident_ctas(size_t sm) {
+  auto k = adjoint_block_kernel<CT, TILE, DMAX>;
+  int per_sm = 0;
+  // without a usable device (host-only plan building) assume one CTA per SM
+  if ((sm > 48 * 1024 &&
+       cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, TILE, sm) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  return per_sm * fock_num_sms();
+}
+
+static int adj_resident(int dtype, int D) {
+  const size_t sm = adjoint_smem(dtype, D);
+  const int b = dmax_bucket(D);
+  if (dtype == FOCK_C64) {
+    switch (b) {
+      case 4: return resident_ctas<float2, 256, 4>(sm);
+      case 8: return resident_ctas<float2, 256, 8>(sm);
+      case 12: return resident_ctas<float2, 256, 12>(sm);
+      case 16: return resident_ctas<float2, 256, 16>(sm);
+      case 20: return resident_ctas<float2, 256, 20>(sm);
+      case 24: return resident_ctas<float2, 256, 24>(sm);
+      default: return resident_ctas<float2, 256, 0>(sm);
+    }
+  }
+  switch (b) {
+    case 4: return resident_ctas<double2, 128, 4>(sm);
+    case 8: return resident_ctas<double2, 128, 8>(sm);
+    case 12: return resident_ctas<double2, 128, 12>(sm);
+    case 16: return resident_ctas<double2, 128, 16>(sm);
+    case 20: return resident_ctas<double2, 128, 20>(sm);
+    case 24: return resident_ctas<double2, 128, 24>(sm);
+    default: return resident_ctas<double2, 128, 0>(sm);
+  }
+}
+
+AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout) {
+  AdjSched sc;
+  memset(&sc, 0, sizeof(sc));
+  sc.nblk = layout == LAYOUT_DENSE ? 1 : 2 * D - 1;
   const int64_t ntiles = (v.ncols + tile_of(dtype) - 1) / tile_of(dtype);
-  // about 8 CTAs per SM in total: several waves, largest blocks scheduled first
-  int target = (8 * fock_num_sms() + nblk - 1) / nblk;
-  if (target < 1) target = 1;
-  int64_t g = ntiles < target ? ntiles : target;
-  return (int)(g < 1 ? 1 : g);
+  // the same number of CTAs for every block (small blocks are memory-bound
+  // and need as many as large ones), about 8 CTAs per SM in total; largest
+  // blocks come first in the flat grid so they start first
+  const int target = 8 * fock_num_sms();
+  (void)adj_resident;
+  int64_t part = 0;
+  int start = 0;
+  for (int y = 0; y < sc.nblk; ++y) {
+    int64_t g = (target + sc.nblk - 1) / sc.nblk;
+    if (g < 1) g = 1;
+    if (g > ntiles) g = ntiles;
+    sc.gx[y] = (int)g;
+    sc.start[y] = start;
+    start += (int)g;
+  }
+  sc.start[sc.nblk] = start;
+  sc.total = start;
+  // partial offsets by stored block index (gx depends only on the block size,
+  // so a block and its mirror image have the same count)
+  for (int bs = 0; bs < sc.nblk; ++bs) {
+    const int s = layout == LAYOUT_DENSE ? D : blk_size(D, bs);
+    // gx of a view block of the same size
+    int g = 1;
+    for (int y = 0; y < sc.nblk; ++y)
+      if ((layout == LAYOUT_DENSE ? D : blk_size(D, block_of_y(D, y))) == s) { g = sc.gx[y]; break; }
+    sc.part_off[bs] = part;
+    part += (int64_t)g * s * s;
+  }
+  sc.part_entries = part;
+  return sc;
 }
 
-int64_t adjoint_scratch_entries(int dtype, const AxisView& v, int D, int layout) {
-  return (int64_t)adjoint_grid_x(dtype, v, D, layout) * layout_entries(layout, D);
+__global__ void reduce_sched_kernel(const double2* __restrict__ cpart, AdjSched sc, int D, int layout,
+                                    double2* __restrict__ cout, int64_t part_stride, int64_t out_stride) {
+  const int lane = threadIdx.x & 31;
+  const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  cpart += blockIdx.y * part_stride;
+  cout += blockIdx.y * out_stride;
+  const int64_t nent = layout == LAYOUT_DENSE ? (int64_t)D * D : blk_total(D);
+  if (e >= nent) return;
+  // stored block of entry e
+  int bs = 0;
+  int64_t off = 0;
+  int s = D;
+  if (layout != LAYOUT_DENSE) {
+    for (bs = 0; bs < 2 * D - 1; ++bs) {
+      s = blk_size(D, bs);
+      if (e < off + (int64_t)s * s) break;
+      off += (int64_t)s * s;
+    }
+  }
+  int g = 1;
+  for (int y = 0; y < sc.nblk; ++y)
+    if ((layout == LAYOUT_DENSE ? D : blk_size(D, block_of_y(D, y))) == s) { g = sc.gx[y]; break; }
+  const int64_t le = e - off;
+  double2 a = make_double2(0.0, 0.0);
+  for (int x = lane; x < g; x += 32) {
+    double2 p = cpart[sc.part_off[bs] + (int64_t)x * s * s + le];
+    a.x += p.x;
+    a.y += p.y;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
+    a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
+  }
+  if (lane == 0) cout[e] = a;
+}
+
+int launch_reduce_sched(const double2* cpart, const AdjSched& sc, int D, int layout, double2* cout, cudaStream_t st,
+                        int nb, int64_t part_stride, int64_t out_stride) {
+  const int64_t nent = layout == LAYOUT_DENSE ? (int64_t)D * D : blk_total(D);
+  const int64_t blocks = (nent * 32 + 255) / 256;
+  reduce_sched_kernel<<<dim3((unsigned)blocks, nb), 256, 0, st>>>(cpart, sc, D, layout, cout, part_stride,
+                                                                  out_stride);
+  FOCK_LAUNCH_CHECK("reduce_sched_kernel");
+  return FOCK_OK;
 }
 
 template <typename CT, int TILE, int DMAX>
 static int launch_adj_t(const void* psi_in, const void* lam_out, void* lam_in, const AxisView& v, int D,
-                        int layout, const double2* mat, int mflags, double2* cpart, int gx, size_t sm,
+                        int layout, const double2* mat, int mflags, double2* cpart, const AdjSched& sc, size_t sm,
                         cudaStream_t st, const BatchArg& bt) {
-  const int nblk = layout == LAYOUT_DENSE ? 1 : 2 * D - 1;
   if (bt.nb < 1 || bt.nb > 65535) return fock_set_error(FOCK_ERR_INVALID, "batch of %d circuits", bt.nb);
-  const int64_t nent = layout_entries(layout, D);
   auto k = adjoint_block_kernel<CT, TILE, DMAX>;
   if (sm > 48 * 1024) FOCK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  dim3 grid(gx, nblk, bt.nb);
-  k<<<grid, TILE, sm, st>>>((const CT*)psi_in, (const CT*)lam_out, (CT*)lam_in, v, D, layout, mat, mflags, cpart,
-                            nent, lam_in != nullptr, bt);
+  dim3 grid(sc.total, 1, bt.nb);
+  k<<<grid, TILE, sm, st>>>((const CT*)psi_in, (const CT*)lam_out, (CT*)lam_in, v, D, layout, mat, mflags, cpart, sc,
+                            lam_in != nullptr, bt);
   FOCK_LAUNCH_CHECK("adjoint_block_kernel");
   return FOCK_OK;
 }
 
 template <typename CT, int TILE>
 static int launch_adj_d(const void* psi_in, const void* lam_out, void* lam_in, const AxisView& v, int D,
-                        int layout, const double2* mat, int mflags, double2* cpart, int gx, size_t sm,
+                        int layout, const double2* mat, int mflags, double2* cpart, const AdjSched& sc, size_t sm,
                         cudaStream_t st, const BatchArg& bt) {
   switch (dmax_bucket(D)) {
-    case 4: return launch_adj_t<CT, TILE, 4>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, gx, sm, st, bt);
-    case 8: return launch_adj_t<CT, TILE, 8>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, gx, sm, st, bt);
-    case 12: return launch_adj_t<CT, TILE, 12>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, gx, sm, st, bt);
-    case 16: return launch_adj_t<CT, TILE, 16>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, gx, sm, st, bt);
-    case 20: return launch_adj_t<CT, TILE, 20>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, gx, sm, st, bt);
-    case 24: return launch_adj_t<CT, TILE, 24>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, gx, sm, st, bt);
-    default: return launch_adj_t<CT, TILE, 0>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, gx, sm, st, bt);
+    case 4: return launch_adj_t<CT, TILE, 4>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, sc, sm, st, bt);
+    case 8: return launch_adj_t<CT, TILE, 8>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, sc, sm, st, bt);
+    case 12: return launch_adj_t<CT, TILE, 12>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, sc, sm, st, bt);
+    case 16: return launch_adj_t<CT, TILE, 16>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, sc, sm, st, bt);
+    case 20: return launch_adj_t<CT, TILE, 20>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, sc, sm, st, bt);
+    case 24: return launch_adj_t<CT, TILE, 24>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, sc, sm, st, bt);
+    default: return launch_adj_t<CT, TILE, 0>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, sc, sm, st, bt);
   }
 }
 
 int launch_adjoint_partials(int dtype, const void* psi_in, const void* lam_out, void* lam_in,
                             const AxisView& v, int D, int layout, const double2* mat, int mflags,
-                            double2* cpart, int gx, cudaStream_t st, const BatchArg& bt) {
+                            double2* cpart, const AdjSched& sc, cudaStream_t st, const BatchArg& bt) {
   const size_t sm = adjoint_smem(dtype, D);
   if (dtype == FOCK_C64)
-    return launch_adj_d<float2, 256>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, gx, sm, st, bt);
-  return launch_adj_d<double2, 128>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, gx, sm, st, bt);
+    return launch_adj_d<float2, 256>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, sc, sm, st, bt);
+  return launch_adj_d<double2, 128>(psi_in, lam_out, lam_in, v, D, layout, mat, mflags, cpart, sc, sm, st, bt);
 }
 
 // cout[e] = sum_x cpart[x][e]  (one warp per entry, fixed summation order)
 __global__ void reduce_partials_kernel(const double2* __restrict__ cpart, int gx, int64_t nent,
-                                       double2* __restrict__ cout) {
+                                       double2* __restrict__ cout, int64_t part_stride, int64_t out_stride) {
   const int lane = threadIdx.x & 31;
+  // blockIdx.y: circuit of a batch
+  cpart += blockIdx.y * part_stride;
+  cout += blockIdx.y * out_stride;
   const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (e >= nent) return;
   double2 a = make_double2(0.0, 0.0);
@@ -293,10 +427,12 @@ __global__ void reduce_partials_kernel(const double2* __restrict__ cpart, int gx
   if (lane == 0) cout[e] = a;
 }
 
-int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* cout, cudaStream_t st) {
+int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* cout, cudaStream_t st, int nb,
+                           int64_t part_stride, int64_t out_stride) {
   const int64_t threads = nent * 32;
   const int64_t blocks = (threads + 255) / 256;
-  reduce_partials_kernel<<<(unsigned)blocks, 256, 0, st>>>(cpart, gx, nent, cout);
+  reduce_partials_kernel<<<dim3((unsigned)blocks, nb), 256, 0, st>>>(cpart, gx, nent, cout, part_stride,
+                                                                      out_stride);
   FOCK_LAUNCH_CHECK("reduce_partials_kernel");
   return FOCK_OK;
 }

@@ -4,16 +4,16 @@
 // D x D block (single-mode gates) or as 2D-1 photon-number blocks (beamsplitter
 // / MZ conserve n1+n2, two-mode squeezing and the loss superoperator conserve
 // n1-n2 -- the selection rules the reference exploits in
-// fockbackend/circuit.py:307-365).  Grid: x over column pairs, y over blocks
-// (largest first).  Each thread takes two columns (j and j + 256 of its
-// CTA's 512-column slice): it loads the s values of its block for both into
-// registers (coalesced across the warp: consecutive threads take consecutive
-// columns, i.e. consecutive addresses along the innermost non-gate axis),
-// multiplies by the s x s block held in shared memory -- every matrix entry
-// read from shared memory feeds both columns -- and stores 2 s outputs.  The
-// kernel is compiled per cutoff bucket DMAX so its register budget matches the
-// largest block it can meet; block sizes are compile-time constants through a
-// dispatch chain, so loads and complex FMAs are fully unrolled.
+// fockbackend/circuit.py:307-365).  Grid: x over columns, y over blocks
+// (largest first).  Each thread takes one column: it loads the s values of
+// its block into registers (coalesced across the warp: consecutive threads
+// take consecutive columns, i.e. consecutive addresses along the innermost
+// non-gate axis), multiplies by the s x s block held in shared memory
+// (broadcast reads) and stores s outputs.  The kernel is compiled per cutoff
+// bucket DMAX so its register budget allows 4 resident CTAs (32 warps) per
+// SM -- the other warps' loads hide each warp's memory latency; block sizes
+// are compile-time constants through a dispatch chain, so loads and complex
+// FMAs are fully unrolled.
 #include "apply.cuh"
 
 AxisView make_view1(int naxes, int D, int ax) {
@@ -41,39 +41,39 @@ AxisView make_view2(int naxes, int D, int ax1, int ax2) {
 }
 
 #define APPLY_THREADS 256
-#define APPLY_COLS 2
+#define APPLY_COLS 1
 
+// The column's loads are issued before the block is staged in shared memory,
+// so the two global round trips overlap.
 template <typename CT, int S>
 __device__ __forceinline__ void apply_cols(const CT* __restrict__ in, CT* __restrict__ out,
-                                           const AxisView& v, int D, const CT* Ms,
+                                           const AxisView& v, int D, CT* Ms, const double2* mat, int mflags,
                                            const BlockGeom& g, int64_t j0) {
-  const int64_t j1 = j0 + APPLY_THREADS;
-  const bool has1 = j1 < v.ncols;
-  const int64_t b0 = col_base(v, j0, D) + g.boff;
-  const int64_t b1 = has1 ? col_base(v, j1, D) + g.boff : b0;
-  CT x0[S], x1[S];
+  const bool valid = j0 < v.ncols;
+  const int64_t b0 = valid ? col_base(v, j0, D) + g.boff : 0;
+  CT x0[S];
+  if (valid) {
 #pragma unroll
-  for (int u = 0; u < S; ++u) {
-    x0[u] = __ldg(in + b0 + u * g.step);
-    x1[u] = __ldg(in + b1 + u * g.step);
+    for (int u = 0; u < S; ++u) x0[u] = __ldg(in + b0 + u * g.step);
   }
+  stage_block(Ms, mat, g, mflags);
+  __syncthreads();
+  if (!valid) return;
 #pragma unroll
   for (int w = 0; w < S; ++w) {
-    CT a0 = czero<CT>(), a1 = czero<CT>();
+    CT a0 = czero<CT>();
 #pragma unroll
-    for (int u = 0; u < S; ++u) {
-      const CT m = Ms[w * S + u];
-      cfma(a0, m, x0[u]);
-      cfma(a1, m, x1[u]);
-    }
+    for (int u = 0; u < S; ++u) cfma(a0, Ms[w * S + u], x0[u]);
     out[b0 + w * g.step] = a0;
-    if (has1) out[b1 + w * g.step] = a1;
   }
 }
 
 template <typename CT>
 __device__ void apply_cols_generic(const CT* __restrict__ in, CT* __restrict__ out, const AxisView& v,
-                                   int D, const CT* Ms, const BlockGeom& g, int64_t j0) {
+                                   int D, CT* Ms, const double2* mat, int mflags, const BlockGeom& g,
+                                   int64_t j0) {
+  stage_block(Ms, mat, g, mflags);
+  __syncthreads();
   for (int k = 0; k < APPLY_COLS; ++k) {
     const int64_t j = j0 + k * APPLY_THREADS;
     if (j >= v.ncols) break;
@@ -90,26 +90,27 @@ __device__ void apply_cols_generic(const CT* __restrict__ in, CT* __restrict__ o
 // s == S ? run the unrolled body : try S + 1 (up to DMAX)
 template <typename CT, int S, int DMAX>
 struct ApplyDispatch {
-  __device__ __forceinline__ static void run(const CT* in, CT* out, const AxisView& v, int D, const CT* Ms,
-                                             const BlockGeom& g, int64_t j0) {
-    if (g.s == S) apply_cols<CT, S>(in, out, v, D, Ms, g, j0);
-    else ApplyDispatch<CT, S + 1, DMAX>::run(in, out, v, D, Ms, g, j0);
+  __device__ __forceinline__ static void run(const CT* in, CT* out, const AxisView& v, int D, CT* Ms,
+                                             const double2* mat, int mflags, const BlockGeom& g, int64_t j0) {
+    if (g.s == S) apply_cols<CT, S>(in, out, v, D, Ms, mat, mflags, g, j0);
+    else ApplyDispatch<CT, S + 1, DMAX>::run(in, out, v, D, Ms, mat, mflags, g, j0);
   }
 };
 template <typename CT, int DMAX>
 struct ApplyDispatch<CT, DMAX + 1, DMAX> {
-  __device__ __forceinline__ static void run(const CT* in, CT* out, const AxisView& v, int D, const CT* Ms,
-                                             const BlockGeom& g, int64_t j0) {
-    apply_cols_generic<CT>(in, out, v, D, Ms, g, j0);
+  __device__ __forceinline__ static void run(const CT* in, CT* out, const AxisView& v, int D, CT* Ms,
+                                             const double2* mat, int mflags, const BlockGeom& g, int64_t j0) {
+    apply_cols_generic<CT>(in, out, v, D, Ms, mat, mflags, g, j0);
   }
 };
 
+// 4 resident CTAs (32 warps) per SM for cutoffs up to 12, 2 beyond
+template <int DMAX> struct ApplyMinBlocks { static const int value = (DMAX > 0 && DMAX <= 12) ? 4 : 2; };
+
 template <typename CT, int DMAX>
-__global__ void __launch_bounds__(APPLY_THREADS) apply_block_kernel(const CT* __restrict__ in,
-                                                                    CT* __restrict__ out, AxisView v, int D,
-                                                                    int layout,
-                                                                    const double2* __restrict__ mat,
-                                                                    int mflags, BatchArg bt) {
+__global__ void __launch_bounds__(APPLY_THREADS, ApplyMinBlocks<DMAX>::value) apply_block_kernel(
+    const CT* __restrict__ in, CT* __restrict__ out, AxisView v, int D, int layout, const double2* __restrict__ mat,
+    int mflags, BatchArg bt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   CT* Ms = reinterpret_cast<CT*>(smem_raw);
   in += blockIdx.z * bt.state_stride;
@@ -117,11 +118,8 @@ __global__ void __launch_bounds__(APPLY_THREADS) apply_block_kernel(const CT* __
   mat += blockIdx.z * bt.mat_stride;
   const int b = layout == LAYOUT_DENSE ? 0 : block_of_y(D, blockIdx.y);
   const BlockGeom g = block_geom(v, D, layout, b, (mflags & MF_SWAP) ? 1 : 0);
-  stage_block(Ms, mat, g, mflags);
-  __syncthreads();
   const int64_t j0 = (int64_t)blockIdx.x * (APPLY_THREADS * APPLY_COLS) + threadIdx.x;
-  if (j0 >= v.ncols) return;
-  ApplyDispatch<CT, 1, DMAX>::run(in, out, v, D, Ms, g, j0);
+  ApplyDispatch<CT, 1, DMAX>::run(in, out, v, D, Ms, mat, mflags, g, j0);
 }
 
 template <typename CT, int DMAX>

@@ -110,12 +110,69 @@ int launch_apply(int dtype, const void* in, void* out, const AxisView& v, int D,
 // C[u][v] = sum over columns conj(lam_out[u]) psi_in[v] (stored-matrix
 // orientation, FP64), written to cpart[gx][entries] with gx =
 // adjoint_grid_x(...).  launch_reduce_partials sums them in a fixed order.
+// CTA schedule of one adjoint launch: block b (view orientation) gets gx[b]
+// persistent CTAs, in proportion to its s_b^2 work; CTAs start[b] ..
+// start[b+1]-1 serve it.  Partial sums of stored-orientation block bs sit at
+// part_off[bs] + x * s^2 (x < gx of that size).
+#define ADJ_MAX_BLOCKS 48
+struct AdjSched {
+  int nblk;
+  int total;
+  int64_t part_entries;
+  int gx[ADJ_MAX_BLOCKS];
+  int start[ADJ_MAX_BLOCKS + 1];
+  int64_t part_off[ADJ_MAX_BLOCKS];
+};
+AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout);
 int launch_adjoint_partials(int dtype, const void* psi_in, const void* lam_out, void* lam_in,
                             const AxisView& v, int D, int layout, const double2* mat, int mflags,
-                            double2* cpart, int gx, cudaStream_t st, const BatchArg& bt = BatchArg());
-int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* cout, cudaStream_t st);
-int64_t adjoint_scratch_entries(int dtype, const AxisView& v, int D, int layout);
-int adjoint_grid_x(int dtype, const AxisView& v, int D, int layout);
+                            double2* cpart, const AdjSched& sc, cudaStream_t st, const BatchArg& bt = BatchArg());
+int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* cout, cudaStream_t st, int nb = 1,
+                           int64_t part_stride = 0, int64_t out_stride = 0);
+// sum the partials of a schedule into `cout` (stored orientation, layout entries)
+int launch_reduce_sched(const double2* cpart, const AdjSched& sc, int D, int layout, double2* cout, cudaStream_t st,
+                        int nb = 1, int64_t part_stride = 0, int64_t out_stride = 0);
+
+// Plane-tile kernels (plane.cu): a persistent CTA stages TC columns' whole
+// planes (D elements for one mode, D x D for two) in shared memory and applies
+// every block of the op to them.  The geometry is built once per op on the
+// host and passed by value.
+#define PL_THREADS 256
+#define PL_WARPS 8
+#define PL_MAX_BLK 48
+#define PL_MAX_ITEMS 128
+#define PL_MAX_D1 24  // one-mode ops up to this cutoff
+#define PL_MAX_D2 16  // two-mode ops up to this cutoff (D*D <= PL_THREADS rows)
+struct PlaneGeom {
+  int64_t A, B, C, s1, s2, ncols, ntiles;  // view [A][D][B][D][C] and its columns
+  int D, E, EP, TC;       // cutoff, plane elements, padded row, columns per tile
+  int two, c_inner;       // two-mode plane; copy with lanes over columns
+  int flat;               // plane of column j starts at j*E (gate on the innermost axes)
+  unsigned emagic;        // ceil(2^26 / E): idx / E as a multiply-shift
+  int nblk, nrows, G;     // blocks, C rows (sum of sizes), column groups of the C pass
+  int nent, ms_total;     // C entries (= staged matrix entries)
+  int sm_goff, sm_cb, sm_tile, smem;  // shared-memory layout (bytes)
+  short base[PL_MAX_BLK], step[PL_MAX_BLK], s[PL_MAX_BLK];  // block y: elements base + u*step
+  int ms_off[PL_MAX_BLK + 1];  // staged matrix of block y (prefix of s^2)
+  int moff[PL_MAX_BLK];        // stored matrix offset of block y
+  int cout_off[PL_MAX_BLK];    // offset of block y's C entries (stored orientation)
+  unsigned char rev[PL_MAX_BLK];
+  unsigned char rows_y[PL_THREADS], rows_u[PL_THREADS];  // C row -> (block, position)
+  short warp_start[PL_WARPS + 1];
+  unsigned short items[PL_MAX_ITEMS];  // (block << 4) | column group, per warp
+};
+// 0 when the op does not fit the plane kernels (then the block kernels run)
+int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, int adjoint, PlaneGeom* g);
+int plane_grid(int dtype, const PlaneGeom& g, int adjoint, int nb);
+// the ops the plane kernels run by default (the others keep the block kernels)
+int plane_preferred(int layout, const AxisView& v);
+int launch_plane_apply(int dtype, const void* in, void* out, const PlaneGeom& g, int grid, const double2* mat,
+                       int mflags, cudaStream_t st, const BatchArg& bt = BatchArg());
+// lam_in = M^dagger lam_out (skipped when lam_in is null) and per-CTA partial
+// C sums in cpart[grid][g.nent]; reduce with launch_reduce_partials(gx = grid)
+int launch_plane_adjoint(int dtype, const void* psi_in, const void* lam_out, void* lam_in, const PlaneGeom& g,
+                         int grid, const double2* mat, int mflags, double2* cpart, cudaStream_t st,
+                         const BatchArg& bt = BatchArg());
 
 // reduced density matrix pieces (capi.cu)
 int launch_rdm_mixed(int dtype, const void* state, int num_modes, int D, int mode, int64_t ntr, int chunks,

@@ -77,33 +77,43 @@ static AxisView mode_view(int naxes, int D, int a1, int a2, int* swap) {
 }
 
 // apply an already-built matrix (layout) to a pure or mixed state
+// out = M in on one view: the plane-tile kernel for the ops it is preferred
+// for, else the block-per-CTA kernel
+static int apply_view(int dtype, const void* in, void* out, const AxisView& v, int D, int layout,
+                      const double2* M, int mflags, cudaStream_t st) {
+  PlaneGeom g;
+  if (plane_preferred(layout, v) && make_plane_geom(dtype, v, D, layout, (mflags & MF_SWAP) ? 1 : 0, 0, &g))
+    return launch_plane_apply(dtype, in, out, g, plane_grid(dtype, g, 0, 1), M, mflags, st);
+  return launch_apply(dtype, in, out, v, D, layout, M, mflags, st);
+}
+
 static int apply_built(const double2* M, int layout, int mode1, int mode2, int num_modes, int D, int pure,
                        int dtype, const void* in, void* out, void* tmp, int is_channel, cudaStream_t st) {
   int swap = 0;
   if (pure) {
     AxisView v = mode_view(num_modes, D, mode1, layout == LAYOUT_DENSE ? -1 : mode2, &swap);
-    return launch_apply(dtype, in, out, v, D, layout, M, swap ? MF_SWAP : 0, st);
+    return apply_view(dtype, in, out, v, D, layout, M, swap ? MF_SWAP : 0, st);
   }
   const int naxes = 2 * num_modes;
   if (is_channel) {
     // superoperator on the (ket, bra) axis pair of one mode
     AxisView v = make_view2(naxes, D, 2 * mode1, 2 * mode1 + 1);
-    return launch_apply(dtype, in, out, v, D, layout, M, 0, st);
+    return apply_view(dtype, in, out, v, D, layout, M, 0, st);
   }
   if (!tmp) return fock_set_error(FOCK_ERR_INVALID, "mixed states need a temporary state buffer");
   int rc;
   if (layout == LAYOUT_DENSE) {
     AxisView vk = make_view1(naxes, D, 2 * mode1);
-    rc = launch_apply(dtype, in, tmp, vk, D, layout, M, 0, st);
+    rc = apply_view(dtype, in, tmp, vk, D, layout, M, 0, st);
     if (rc) return rc;
     AxisView vb = make_view1(naxes, D, 2 * mode1 + 1);
-    return launch_apply(dtype, tmp, out, vb, D, layout, M, MF_CONJ, st);
+    return apply_view(dtype, tmp, out, vb, D, layout, M, MF_CONJ, st);
   }
   AxisView vk = mode_view(naxes, D, 2 * mode1, 2 * mode2, &swap);
-  rc = launch_apply(dtype, in, tmp, vk, D, layout, M, swap ? MF_SWAP : 0, st);
+  rc = apply_view(dtype, in, tmp, vk, D, layout, M, swap ? MF_SWAP : 0, st);
   if (rc) return rc;
   AxisView vb = mode_view(naxes, D, 2 * mode1 + 1, 2 * mode2 + 1, &swap);
-  return launch_apply(dtype, tmp, out, vb, D, layout, M, MF_CONJ | (swap ? MF_SWAP : 0), st);
+  return apply_view(dtype, tmp, out, vb, D, layout, M, MF_CONJ | (swap ? MF_SWAP : 0), st);
 }
 
 // ---------------------------------------------------------------------------
@@ -630,15 +640,12 @@ int check_reduced_dm1_args(int num_modes, int cutoff, int pure, int dtype, int m
 extern "C" int64_t fock_reduced_dm1_workspace_bytes(int num_modes, int cutoff, int pure, int dtype) {
   int64_t c = (int64_t)cutoff * cutoff;
   if (pure) {
-    AxisView v = make_view1(num_modes, cutoff, 0);
-    int64_t g = 0;
+    int64_t part = 0;
     for (int m = 0; m < num_modes; ++m) {
-      AxisView vm = make_view1(num_modes, cutoff, m);
-      int64_t gm = adjoint_grid_x(dtype, vm, cutoff, LAYOUT_DENSE);
-      if (gm > g) g = gm;
+      AdjSched sc = make_adj_sched(dtype, make_view1(num_modes, cutoff, m), cutoff, LAYOUT_DENSE);
+      if (sc.part_entries > part) part = sc.part_entries;
     }
-    (void)v;
-    return (g + 1) * c * 16 + 256;
+    return (part + c) * 16 + 256;
   }
   return (64 + 1) * c * 16 + 256;
 }
@@ -656,13 +663,13 @@ extern "C" int fock_reduced_dm1(int num_modes, int cutoff, int pure, int dtype, 
   if (pure) {
     // C[u][v] = sum conj(psi[u]) psi[v] = rho[v][u]
     AxisView v = make_view1(num_modes, D, mode);
-    const int gx = adjoint_grid_x(dtype, v, D, LAYOUT_DENSE);
+    const AdjSched sc = make_adj_sched(dtype, v, D, LAYOUT_DENSE);
     double2* C = ws;
     double2* cpart = ws + (int64_t)D * D;
-    // identity matrix is not needed (lam_in not written); pass a dummy pointer
-    rc = launch_adjoint_partials(dtype, state, state, nullptr, v, D, LAYOUT_DENSE, C, 0, cpart, gx, st);
+    // the matrix is not needed (lam_in not written); pass any in-bounds pointer
+    rc = launch_adjoint_partials(dtype, state, state, nullptr, v, D, LAYOUT_DENSE, C, 0, cpart, sc, st);
     if (rc) return rc;
-    rc = launch_reduce_partials(cpart, gx, (int64_t)D * D, C, st);
+    rc = launch_reduce_sched(cpart, sc, D, LAYOUT_DENSE, C, st);
     if (rc) return rc;
     transpose_dm_kernel<<<1, 256, 0, st>>>(C, (double2*)out, D);
     FOCK_LAUNCH_CHECK("transpose_dm_kernel");

@@ -58,13 +58,18 @@ extern "C" int fock_reduced_dm1_noalloc(int num_modes, int cutoff, int pure, int
     // C[u][v] = sum conj(psi[u]) psi[v] = rho[v][u]; every partial slot the
     // grid uses is written before it is read, so nothing needs clearing
     AxisView v = make_view1(num_modes, D, mode);
-    int gx = adjoint_grid_x(dtype, v, D, LAYOUT_DENSE);
-    if (gx > slots) gx = (int)slots;
+    AdjSched sc = make_adj_sched(dtype, v, D, LAYOUT_DENSE);
+    if (sc.gx[0] > slots) {
+      // fewer CTAs, each covering more column tiles, so the partials fit
+      sc.gx[0] = (int)slots;
+      sc.start[1] = sc.total = (int)slots;
+      sc.part_entries = slots * (int64_t)D * D;
+    }
     double2* C = scratch;
     double2* cpart = scratch + (int64_t)D * D;
-    rc = launch_adjoint_partials(dtype, state, state, nullptr, v, D, LAYOUT_DENSE, C, 0, cpart, gx, st);
+    rc = launch_adjoint_partials(dtype, state, state, nullptr, v, D, LAYOUT_DENSE, C, 0, cpart, sc, st);
     if (rc) return rc;
-    if ((rc = launch_reduce_partials(cpart, gx, (int64_t)D * D, C, st))) return rc;
+    if ((rc = launch_reduce_sched(cpart, sc, D, LAYOUT_DENSE, C, st))) return rc;
     return launch_transpose_dm(C, (double2*)out, D, st);
   }
   int64_t ntr = 1;

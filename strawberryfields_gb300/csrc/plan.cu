@@ -15,6 +15,7 @@
 // on every call, so a captured CUDA graph replays them.
 #include "apply.cuh"
 
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -33,14 +34,13 @@ struct PlanOp {
   // derived
   AxisView view;
   int swap = 0;
-  int64_t m_off = 0, dm_off = -1, scratch_off = -1, c_off = 0, cpart_off = 0;
-  int gx = 1;
+  int64_t m_off = 0, dm_off = -1, scratch_off = -1, c_off = 0;
+  AdjSched sched;  // CTA schedule and partial-sum layout of the adjoint launch
   int64_t nent = 0;
-};
-
-struct RedOp {
-  int64_t c_off, cpart_off, nent;
-  int gx, pad_;
+  // plane-tile kernels (when the op fits them): geometry and persistent grids
+  int plane = 0;
+  PlaneGeom pg_fwd, pg_adj;
+  int grid_fwd = 0, grid_adj = 0;
 };
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -54,7 +54,7 @@ struct fock_plan {
   // table image (pinned host memory) and its sections
   unsigned char* host = nullptr;
   size_t tables_bytes = 0;
-  size_t o_jobs = 0, o_terms = 0, o_gops = 0, o_contrib = 0, o_pstart = 0, o_plist = 0, o_red = 0;
+  size_t o_jobs = 0, o_terms = 0, o_gops = 0, o_contrib = 0, o_pstart = 0, o_plist = 0;
   int n_terms = 0, n_contrib = 0;
   // workspace sections
   size_t o_arena = 0, o_carena = 0, o_cpart = 0, ws_bytes = 0;
@@ -67,6 +67,16 @@ struct fock_plan {
   int fwd_recorded = 0, bwd_recorded = 0;
 };
 
+// Record a timing event; inside a stream capture it must be an external
+// event-record node so that elapsed times can be read after each replay.
+static int record_event(cudaEvent_t ev, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  FOCK_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+  if (cs == cudaStreamCaptureStatusActive) FOCK_CUDA_TRY(cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal));
+  else FOCK_CUDA_TRY(cudaEventRecord(ev, st));
+  return FOCK_OK;
+}
+
 static int ensure_events(std::vector<cudaEvent_t>& ev, size_t n) {
   while (ev.size() < n) {
     cudaEvent_t e;
@@ -74,40 +84,6 @@ static int ensure_events(std::vector<cudaEvent_t>& ev, size_t n) {
     ev.push_back(e);
   }
   return FOCK_OK;
-}
-
-// ---------------------------------------------------------------------------
-// batched reduction of all ops' partial C sums
-// ---------------------------------------------------------------------------
-__global__ void reduce_all_kernel(const RedOp* __restrict__ ops, int n_ops, int64_t total,
-                                  const double2* __restrict__ cpart, double2* __restrict__ carena,
-                                  int64_t cpart_stride) {
-  const int lane = threadIdx.x & 31;
-  int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  // blockIdx.y: circuit of a batch
-  cpart += blockIdx.y * cpart_stride;
-  carena += blockIdx.y * total;
-  if (e >= total) return;
-  int lo = 0, hi = n_ops - 1;
-  while (lo < hi) {  // last op with c_off <= e
-    int mid = (lo + hi + 1) >> 1;
-    if (ops[mid].c_off <= e) lo = mid;
-    else hi = mid - 1;
-  }
-  const RedOp R = ops[lo];
-  const int64_t le = e - R.c_off;
-  double2 a = make_double2(0.0, 0.0);
-  for (int x = lane; x < R.gx; x += 32) {
-    double2 p = cpart[R.cpart_off + (int64_t)x * R.nent + le];
-    a.x += p.x;
-    a.y += p.y;
-  }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    a.x += __shfl_xor_sync(0xffffffffu, a.x, off);
-    a.y += __shfl_xor_sync(0xffffffffu, a.y, off);
-  }
-  if (lane == 0) carena[e] = a;
 }
 
 // ---------------------------------------------------------------------------
@@ -312,6 +288,11 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   int64_t elems = 1;
   for (int k = 0; k < N; ++k) elems *= D;
   P->state_elems = elems;
+  // kernel family per op: plane-tile kernels where plane_preferred says so;
+  // FOCK_GB300_KERNELS=block / plane forces one family (where it applies)
+  const char* kern = getenv("FOCK_GB300_KERNELS");
+  const bool use_plane = !(kern && strcmp(kern, "block") == 0);
+  const bool force_plane = kern && strcmp(kern, "plane") == 0;
   int64_t arena = 0, carena = 0, cpart = 0;
   int n_terms = 0, n_contrib = 0;
   for (size_t k = 0; k < P->ops.size(); ++k) {
@@ -329,11 +310,18 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
       op.swap = a > b;
       op.view = make_view2(N, D, std::min(a, b), std::max(a, b));
     }
-    op.gx = adjoint_grid_x(dtype, op.view, D, op.layout);
+    op.sched = make_adj_sched(dtype, op.view, D, op.layout);
+    op.plane = use_plane && (force_plane || plane_preferred(op.layout, op.view)) && make_plane_geom(dtype, op.view, D, op.layout, op.swap, 0, &op.pg_fwd) &&
+               make_plane_geom(dtype, op.view, D, op.layout, op.swap, 1, &op.pg_adj);
+    if (op.plane) {
+      op.grid_fwd = plane_grid(dtype, op.pg_fwd, 0, batch);
+      op.grid_adj = plane_grid(dtype, op.pg_adj, 1, batch);
+    }
     op.c_off = carena;
     carena += op.nent;
-    op.cpart_off = cpart;
-    cpart += (int64_t)op.gx * op.nent;
+    // one partial-sum region shared by all ops: each op's partials are
+    // reduced right after its adjoint launch
+    cpart = std::max<int64_t>(cpart, op.plane ? (int64_t)op.grid_adj * op.pg_adj.nent : op.sched.part_entries);
     n_terms += (int)op.terms.size();
     n_contrib += (int)op.contribs.size();
     // flops: 8 real flops per complex multiply-add
@@ -353,7 +341,6 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   P->o_contrib = o; o = align256(o + sizeof(GradContrib) * std::max(n_contrib, 1));
   P->o_pstart = o; o = align256(o + sizeof(int) * (n_params + 1));
   P->o_plist = o; o = align256(o + sizeof(int) * std::max(n_contrib, 1));
-  P->o_red = o; o = align256(o + sizeof(RedOp) * std::max(n_ops, 1));
   P->tables_bytes = o;
   P->o_arena = o; o = align256(o + sizeof(double2) * arena * batch);
   P->o_carena = o; o = align256(o + sizeof(double2) * std::max<int64_t>(carena, 1) * batch);
@@ -373,7 +360,6 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   GradContrib* contrib = (GradContrib*)(P->host + P->o_contrib);
   int* pstart = (int*)(P->host + P->o_pstart);
   int* plist = (int*)(P->host + P->o_plist);
-  RedOp* red = (RedOp*)(P->host + P->o_red);
   int t = 0, c = 0;
   std::vector<std::vector<int>> by_param(n_params);
   for (int k = 0; k < n_ops; ++k) {
@@ -403,10 +389,6 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
       by_param[gc.pidx].push_back(c);
       ++c;
     }
-    red[k].c_off = op.c_off;
-    red[k].cpart_off = op.cpart_off;
-    red[k].nent = op.nent;
-    red[k].gx = op.gx;
   }
   int q = 0;
   for (int p = 0; p < n_params; ++p) {
@@ -470,22 +452,61 @@ static int upload_and_build(fock_plan* P, const double* params, unsigned char* w
                            params, (double2*)(ws + P->o_arena), st, P->batch, P->n_params, P->arena_entries);
 }
 
+// slot of op j's output in a forward sweep that keeps every k-th state
+// (k = store_every): 0 -> ping-pong slots 0/1; 1 -> slot j; k > 1 -> the
+// checkpoint slot (j+1)/k - 1 when (j+1) % k == 0 or j is the last op,
+// otherwise one of two scratch slots after the n_ckpt checkpoints.
+static int64_t out_slot(int j, int n_ops, int k) {
+  if (k <= 0) return j & 1;
+  if (k == 1) return j;
+  const int64_t nc = (n_ops + k - 1) / k;
+  if ((j + 1) % k == 0) return (j + 1) / k - 1;
+  if (j == n_ops - 1) return nc - 1;
+  return nc + (j & 1);
+}
+
+struct SweepCtx {
+  fock_plan* P;
+  const double2* arena;
+  BatchArg bt;
+  int64_t sb;  // bytes of one slot (whole batch)
+  cudaStream_t st;
+};
+
+static int sweep_ctx(fock_plan* P, unsigned char* ws, cudaStream_t st, SweepCtx* c) {
+  const int esz = P->dtype == FOCK_C64 ? 8 : 16;
+  c->P = P;
+  c->sb = P->state_elems * esz * P->batch;
+  c->arena = (const double2*)(ws + P->o_arena);
+  c->bt.nb = P->batch;
+  c->bt.state_stride = P->state_elems;
+  c->bt.mat_stride = P->arena_entries;
+  c->bt.part_stride = P->cpart_entries;
+  c->st = st;
+  return FOCK_OK;
+}
+
+static int apply_op(const SweepCtx& c, int k, const void* in, void* out) {
+  const PlanOp& op = c.P->ops[k];
+  if (op.plane)
+    return launch_plane_apply(c.P->dtype, in, out, op.pg_fwd, op.grid_fwd, c.arena + op.m_off, op.swap ? MF_SWAP : 0,
+                              c.st, c.bt);
+  return launch_apply(c.P->dtype, in, out, op.view, c.P->D, op.layout, c.arena + op.m_off, op.swap ? MF_SWAP : 0,
+                      c.st, c.bt);
+}
+
 extern "C" int fock_plan_forward(fock_plan* P, const double* params, const void* state_in, void* states,
-                                 int store_all, void* workspace, void* stream) {
+                                 int store_every, void* workspace, void* stream) {
   if (!P) return fock_set_error(FOCK_ERR_INVALID, "null plan");
   if (!state_in || !states || !workspace) return fock_set_error(FOCK_ERR_INVALID, "null buffer");
   if (P->n_params > 0 && !params) return fock_set_error(FOCK_ERR_INVALID, "null parameter array");
+  if (store_every < 0) return fock_set_error(FOCK_ERR_INVALID, "store_every must be >= 0");
   cudaStream_t st = (cudaStream_t)stream;
   unsigned char* ws = (unsigned char*)workspace;
   int rc = upload_and_build(P, params, ws, 0, st);
   if (rc) return rc;
-  const int esz = P->dtype == FOCK_C64 ? 8 : 16;
-  const int64_t sb = P->state_elems * esz * P->batch;  // one op's states for the whole batch
-  const double2* arena = (const double2*)(ws + P->o_arena);
-  BatchArg bt;
-  bt.nb = P->batch;
-  bt.state_stride = P->state_elems;
-  bt.mat_stride = P->arena_entries;
+  SweepCtx c;
+  sweep_ctx(P, ws, st, &c);
   const void* cur = state_in;
   const int n_ops = (int)P->ops.size();
   if (P->timing) {
@@ -493,74 +514,92 @@ extern "C" int fock_plan_forward(fock_plan* P, const double* params, const void*
     P->fwd_recorded = 0;
   }
   for (int k = 0; k < n_ops; ++k) {
-    const PlanOp& op = P->ops[k];
-    void* dst = (char*)states + (store_all ? (int64_t)k : (int64_t)(k & 1)) * sb;
-    if (P->timing) FOCK_CUDA_TRY(cudaEventRecord(P->ev_fwd[k], st));
-    rc = launch_apply(P->dtype, cur, dst, op.view, P->D, op.layout, arena + op.m_off, op.swap ? MF_SWAP : 0, st, bt);
-    if (rc) return rc;
+    void* dst = (char*)states + out_slot(k, n_ops, store_every) * c.sb;
+    if (P->timing && (rc = record_event(P->ev_fwd[k], st))) return rc;
+    if ((rc = apply_op(c, k, cur, dst))) return rc;
     cur = dst;
   }
   if (P->timing) {
-    FOCK_CUDA_TRY(cudaEventRecord(P->ev_fwd[n_ops], st));
+    if ((rc = record_event(P->ev_fwd[n_ops], st))) return rc;
     P->fwd_recorded = 1;
   }
   return FOCK_OK;
 }
 
 extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void* state_in,
-                                  const void* states, void* grad_state, void* grad_tmp, double* grad_params,
-                                  void* workspace, void* stream) {
+                                  const void* states, int store_every, void* seg, void* grad_state,
+                                  void* grad_tmp, double* grad_params, void* workspace, void* stream) {
   if (!P) return fock_set_error(FOCK_ERR_INVALID, "null plan");
   if (!state_in || !states || !grad_state || !grad_tmp || !workspace)
     return fock_set_error(FOCK_ERR_INVALID, "null buffer");
+  if (store_every < 1) return fock_set_error(FOCK_ERR_INVALID, "the adjoint sweep needs store_every >= 1");
+  if (store_every > 1 && !seg) return fock_set_error(FOCK_ERR_INVALID, "checkpointed sweep needs a segment buffer");
   if (P->n_params > 0 && (!params || !grad_params)) return fock_set_error(FOCK_ERR_INVALID, "null parameter array");
   cudaStream_t st = (cudaStream_t)stream;
   unsigned char* ws = (unsigned char*)workspace;
   int rc = upload_and_build(P, params, ws, 1, st);
   if (rc) return rc;
-  const int esz = P->dtype == FOCK_C64 ? 8 : 16;
-  const int64_t sb = P->state_elems * esz * P->batch;
-  const double2* arena = (const double2*)(ws + P->o_arena);
+  SweepCtx c;
+  sweep_ctx(P, ws, st, &c);
   double2* cpart = (double2*)(ws + P->o_cpart);
-  BatchArg bt;
-  bt.nb = P->batch;
-  bt.state_stride = P->state_elems;
-  bt.mat_stride = P->arena_entries;
-  bt.part_stride = P->cpart_entries;
   const int n_ops = (int)P->ops.size();
+  const int K = store_every;
   void* lam = grad_state;
   void* other = grad_tmp;
   if (P->timing) {
     if ((rc = ensure_events(P->ev_bwd, n_ops + 1))) return rc;
     P->bwd_recorded = 0;
   }
-  for (int k = n_ops - 1; k >= 0; --k) {
-    const PlanOp& op = P->ops[k];
-    const void* psi_in = k == 0 ? state_in : (const char*)states + (int64_t)(k - 1) * sb;
-    if (P->timing) FOCK_CUDA_TRY(cudaEventRecord(P->ev_bwd[k + 1], st));
-    rc = launch_adjoint_partials(P->dtype, psi_in, lam, other, op.view, P->D, op.layout, arena + op.m_off,
-                                 op.swap ? MF_SWAP : 0, cpart + op.cpart_off, op.gx, st, bt);
-    if (rc) return rc;
-    void* t = lam;
-    lam = other;
-    other = t;
+  const int nseg = K == 1 ? 1 : (n_ops + K - 1) / K;
+  for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+    const int s0 = K == 1 ? 0 : sgi * K;
+    const int e = K == 1 ? n_ops : std::min(s0 + K, n_ops);
+    const void* seg_in = state_in;
+    if (K > 1) {
+      // recompute the segment's inner states from its checkpoint
+      seg_in = sgi == 0 ? state_in : (const char*)states + (int64_t)(sgi - 1) * c.sb;
+      const void* cur = seg_in;
+      for (int j = s0; j < e - 1; ++j) {
+        void* dst = (char*)seg + (int64_t)(j - s0) * c.sb;
+        if ((rc = apply_op(c, j, cur, dst))) return rc;
+        cur = dst;
+      }
+    }
+    for (int k = e - 1; k >= s0; --k) {
+      const PlanOp& op = P->ops[k];
+      const void* psi_in;
+      if (K == 1) psi_in = k == 0 ? state_in : (const char*)states + (int64_t)(k - 1) * c.sb;
+      else psi_in = k == s0 ? seg_in : (const char*)seg + (int64_t)(k - s0 - 1) * c.sb;
+      if (P->timing && (rc = record_event(P->ev_bwd[k + 1], st))) return rc;
+      double2* cout = (double2*)(ws + P->o_carena) + op.c_off;
+      if (op.plane) {
+        rc = launch_plane_adjoint(P->dtype, psi_in, lam, other, op.pg_adj, op.grid_adj, c.arena + op.m_off,
+                                  op.swap ? MF_SWAP : 0, cpart, st, c.bt);
+        if (rc) return rc;
+        rc = launch_reduce_partials(cpart, op.grid_adj, op.nent, cout, st, P->batch, P->cpart_entries,
+                                    P->carena_entries);
+      } else {
+        rc = launch_adjoint_partials(P->dtype, psi_in, lam, other, op.view, P->D, op.layout, c.arena + op.m_off,
+                                     op.swap ? MF_SWAP : 0, cpart, op.sched, st, c.bt);
+        if (rc) return rc;
+        rc = launch_reduce_sched(cpart, op.sched, P->D, op.layout, cout, st, P->batch, P->cpart_entries,
+                                 P->carena_entries);
+      }
+      if (rc) return rc;
+      void* t = lam;
+      lam = other;
+      other = t;
+    }
   }
   if (P->timing) {
-    FOCK_CUDA_TRY(cudaEventRecord(P->ev_bwd[0], st));
+    if ((rc = record_event(P->ev_bwd[0], st))) return rc;
     P->bwd_recorded = 1;
   }
-  if (lam != grad_state) FOCK_CUDA_TRY(cudaMemcpyAsync(grad_state, lam, sb, cudaMemcpyDeviceToDevice, st));
-  if (n_ops > 0) {
-    const int64_t threads = P->carena_entries * 32;
-    reduce_all_kernel<<<dim3((unsigned)((threads + 255) / 256), P->batch), 256, 0, st>>>(
-        (const RedOp*)(ws + P->o_red), n_ops, P->carena_entries, cpart, (double2*)(ws + P->o_carena),
-        P->cpart_entries);
-    FOCK_LAUNCH_CHECK("reduce_all_kernel");
-  }
+  if (lam != grad_state) FOCK_CUDA_TRY(cudaMemcpyAsync(grad_state, lam, c.sb, cudaMemcpyDeviceToDevice, st));
   if (P->n_params > 0) {
     rc = launch_param_grads((const GradOp*)(ws + P->o_gops), (const GradContrib*)(ws + P->o_contrib),
                             (const int*)(ws + P->o_pstart), (const int*)(ws + P->o_plist), P->n_params,
-                            (const PhaseTerm*)(ws + P->o_terms), arena, (const double2*)(ws + P->o_carena),
+                            (const PhaseTerm*)(ws + P->o_terms), c.arena, (const double2*)(ws + P->o_carena),
                             grad_params, st, P->batch, P->arena_entries, P->carena_entries);
     if (rc) return rc;
   }

@@ -1,0 +1,571 @@
+// Plane-tile kernels: gate apply and adjoint step over whole column planes.
+//
+// A one-mode op sees the state as [A][D][C] and a two-mode op as
+// [A][D][B][D][C]; the D (one mode) or D x D (two modes) elements that share
+// a column j = (a, b, c) form that column's plane.  A persistent CTA takes
+// tiles of TC consecutive columns and
+//   1. copies the tile's planes into shared memory with cp.async, in the
+//      order that keeps global addresses consecutive across a warp (lanes
+//      over columns when the innermost axis C is long, lanes over plane
+//      elements when C is short -- e.g. a beamsplitter on the last two modes,
+//      whose planes are contiguous 2-D blocks);
+//   2. applies every photon-number block of the op to every column from
+//      shared memory (warp = one block for 32 columns; each lane holds one
+//      column's block in registers, the block matrix is broadcast from
+//      shared memory);
+//   3. writes the tile back in the same coalesced order.
+// Every state element therefore crosses HBM exactly once per op whatever
+// the mode pair, the block matrices are staged once per CTA rather than once
+// per (block, column tile), and the next tile's copies are in flight while
+// the current one is computed (two buffers in the apply kernel).
+//
+// The adjoint kernel holds lam_out and psi_in tiles; its C accumulation maps
+// lanes to block rows (thread (b, u) accumulates C_b[u][.] over the tile's
+// columns in registers, psi values broadcast across the rows of a block),
+// then lam_in = M^dagger lam_out is formed in place with the apply mapping
+// and written back.  Per-CTA partial sums of C go to cpart[CTA][entries]
+// (FP64, stored orientation) for a fixed-order reduction.
+//
+// The block structure is the reference's selection rules
+// (strawberryfields/backends/fockbackend/circuit.py:219-365): sum blocks for
+// beamsplitter / MZ, difference blocks for two-mode squeezing and the loss
+// superoperator, one dense block for single-mode gates.
+#include "apply.cuh"
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <string.h>
+#include <tuple>
+#include <vector>
+
+__device__ __forceinline__ void pl_cp(float2* dst, const float2* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src));
+}
+__device__ __forceinline__ void pl_cp(double2* dst, const double2* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src));
+}
+__device__ __forceinline__ void pl_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void pl_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// columns of a tile that starts at column j0 (the last tile may be partial)
+__device__ __forceinline__ int pl_cols(int64_t tc, int64_t rest) { return (int)(rest < tc ? rest : tc); }
+
+__device__ __forceinline__ int64_t pl_col_base(const PlaneGeom& g, int64_t j) {
+  const int64_t c = j % g.C;
+  const int64_t t = j / g.C;
+  const int64_t b = t % g.B;
+  const int64_t a = t / g.B;
+  return a * (g.s1 * g.D) + b * (g.s2 * g.D) + c;
+}
+
+// global offsets of the plane elements (e = i*D + k, or e = i for one mode)
+__device__ __forceinline__ void pl_offsets(int64_t* goff, const PlaneGeom& g) {
+  for (int e = threadIdx.x; e < g.E; e += PL_THREADS)
+    goff[e] = g.two ? (int64_t)(e / g.D) * g.s1 + (int64_t)(e % g.D) * g.s2 : (int64_t)e * g.s1;
+}
+
+// column bases of tile t (the 64-bit index decomposition runs once per
+// column here, not once per copied element)
+__device__ __forceinline__ void pl_bases(int64_t* cb, const PlaneGeom& g, int64_t t) {
+  if (t >= g.ntiles) return;
+  const int64_t j0 = t * g.TC;
+  for (int cc = threadIdx.x; cc < g.TC; cc += PL_THREADS)
+    if (j0 + cc < g.ncols) cb[cc] = pl_col_base(g, j0 + cc);
+}
+
+// column of flat tile index idx (idx / E by multiply-shift; exact for
+// idx < 2^16 and E <= 1024)
+__device__ __forceinline__ int pl_fcol(const PlaneGeom& g, int idx) {
+  return (int)(((uint64_t)(unsigned)idx * (uint64_t)g.emagic) >> 26);
+}
+
+// Issue the copies of the tile's tcv columns (bases cb) into T (row stride EP).
+// Flat tiles (gate on the innermost axes) are one contiguous range.
+template <typename CT>
+__device__ __forceinline__ void pl_issue(const CT* __restrict__ src, CT* T, const PlaneGeom& g,
+                                         const int64_t* goff, const int64_t* cb, int tcv) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (g.flat) {
+    const CT* s = src + cb[0];
+    const int n = tcv * g.E;
+    for (int idx = threadIdx.x; idx < n; idx += PL_THREADS) {
+      const int col = pl_fcol(g, idx);
+      pl_cp(T + col * g.EP + (idx - col * g.E), s + idx);
+    }
+  } else if (g.c_inner) {
+    for (int cc = lane; cc < tcv; cc += 32) {
+      const CT* s = src + cb[cc];
+      CT* row = T + cc * g.EP;
+      for (int e = warp; e < g.E; e += PL_WARPS) pl_cp(row + e, s + goff[e]);
+    }
+  } else {
+    for (int cc = warp; cc < tcv; cc += PL_WARPS) {
+      const CT* s = src + cb[cc];
+      CT* row = T + cc * g.EP;
+      for (int e = lane; e < g.E; e += 32) pl_cp(row + e, s + goff[e]);
+    }
+  }
+  pl_commit();
+}
+
+template <typename CT>
+__device__ __forceinline__ void pl_store(CT* __restrict__ dst, const CT* T, const PlaneGeom& g, const int64_t* goff,
+                                         const int64_t* cb, int tcv) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (g.flat) {
+    CT* d = dst + cb[0];
+    const int n = tcv * g.E;
+    for (int idx = threadIdx.x; idx < n; idx += PL_THREADS) {
+      const int col = pl_fcol(g, idx);
+      d[idx] = T[col * g.EP + (idx - col * g.E)];
+    }
+  } else if (g.c_inner) {
+    for (int cc = lane; cc < tcv; cc += 32) {
+      CT* d = dst + cb[cc];
+      const CT* row = T + cc * g.EP;
+      for (int e = warp; e < g.E; e += PL_WARPS) d[goff[e]] = row[e];
+    }
+  } else {
+    for (int cc = warp; cc < tcv; cc += PL_WARPS) {
+      CT* d = dst + cb[cc];
+      const CT* row = T + cc * g.EP;
+      for (int e = lane; e < g.E; e += 32) d[goff[e]] = row[e];
+    }
+  }
+}
+
+// Stage every block's matrix (view orientation, state precision): forward
+// Ms[w][u] maps view input u to output w; with MF_ADJOINT the conjugate
+// transpose.  Reverse-stored sum blocks (MF_SWAP) read s-1-position.
+template <typename CT>
+__device__ __forceinline__ void pl_stage(CT* Ms, const double2* __restrict__ mat, const PlaneGeom& g, int mflags) {
+  const int cj = ((mflags & MF_ADJOINT) ? 1 : 0) ^ ((mflags & MF_CONJ) ? 1 : 0);
+#pragma unroll 4
+  for (int idx = threadIdx.x; idx < g.ms_total; idx += PL_THREADS) {
+    int y = 0;
+    while (y + 1 < g.nblk && idx >= g.ms_off[y + 1]) ++y;
+    const int s = g.s[y];
+    const int e = idx - g.ms_off[y];
+    const int w = e / s, u = e - w * s;
+    int a = w, c = u;
+    if (mflags & MF_ADJOINT) { a = u; c = w; }
+    if (g.rev[y]) { a = s - 1 - a; c = s - 1 - c; }
+    double2 m = mat[g.moff[y] + a * s + c];
+    if (cj) m.y = -m.y;
+    Ms[idx] = to_c(m, (CT*)nullptr);
+  }
+}
+
+// one column's block: x = Ms x in place (positions base + u*step)
+template <typename CT, int S>
+__device__ __forceinline__ void pl_block(CT* row, int base, int step, const CT* Ms) {
+  CT x[S];
+#pragma unroll
+  for (int u = 0; u < S; ++u) x[u] = row[base + u * step];
+#pragma unroll
+  for (int w = 0; w < S; ++w) {
+    CT a = czero<CT>();
+#pragma unroll
+    for (int u = 0; u < S; ++u) cfma(a, Ms[w * S + u], x[u]);
+    row[base + w * step] = a;
+  }
+}
+template <typename CT, int S, int SMAX>
+struct PlBlock {
+  __device__ __forceinline__ static void run(int s, CT* row, int base, int step, const CT* Ms) {
+    if (s == S) pl_block<CT, S>(row, base, step, Ms);
+    else PlBlock<CT, S + 1, SMAX>::run(s, row, base, step, Ms);
+  }
+};
+template <typename CT, int SMAX>
+struct PlBlock<CT, SMAX + 1, SMAX> {
+  __device__ __forceinline__ static void run(int, CT*, int, int, const CT*) {}
+};
+
+// step 2: every block of every column of the tile (warp items from the host)
+template <typename CT, int SMAX>
+__device__ __forceinline__ void pl_apply_tile(CT* T, const CT* Ms, const PlaneGeom& g, int tcv) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int it = g.warp_start[warp]; it < g.warp_start[warp + 1]; ++it) {
+    const int item = g.items[it];
+    const int y = item >> 4, col = (item & 15) * 32 + lane;
+    if (col < tcv) PlBlock<CT, 1, SMAX>::run(g.s[y], T + col * g.EP, g.base[y], g.step[y], Ms + g.ms_off[y]);
+  }
+}
+
+template <typename CT, int SMAX>
+__global__ void __launch_bounds__(PL_THREADS, 2)
+    plane_apply_kernel(const CT* __restrict__ in, CT* __restrict__ out, const __grid_constant__ PlaneGeom g,
+                       const double2* __restrict__ mat, int mflags, BatchArg bt) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  CT* Ms = reinterpret_cast<CT*>(smem);
+  int64_t* goff = reinterpret_cast<int64_t*>(smem + g.sm_goff);
+  int64_t* cb0 = reinterpret_cast<int64_t*>(smem + g.sm_cb);
+  CT* T0 = reinterpret_cast<CT*>(smem + g.sm_tile);
+  const int64_t tsz = (int64_t)g.TC * g.EP;
+  in += blockIdx.z * bt.state_stride;
+  out += blockIdx.z * bt.state_stride;
+  mat += blockIdx.z * bt.mat_stride;
+  const int64_t G = gridDim.x;
+  int64_t t = blockIdx.x;
+  pl_offsets(goff, g);
+  pl_bases(cb0, g, t);
+  pl_bases(cb0 + g.TC, g, t + G);
+  __syncthreads();
+  if (t < g.ntiles) pl_issue(in, T0, g, goff, cb0, pl_cols(g.TC, g.ncols - t * g.TC));
+  pl_stage(Ms, mat, g, mflags);  // overlaps the first tile's copies
+  int buf = 0;
+  // buffer buf holds tile t (bases cb0 + buf*TC); buf^1 receives tile t + G
+  for (; t < g.ntiles; t += G) {
+    const int64_t tn = t + G;
+    const int tcv = pl_cols(g.TC, g.ncols - t * g.TC);
+    CT* T = T0 + buf * tsz;
+    int64_t* cb = cb0 + buf * g.TC;
+    if (tn < g.ntiles) {
+      pl_issue(in, T0 + (buf ^ 1) * tsz, g, goff, cb0 + (buf ^ 1) * g.TC, pl_cols(g.TC, g.ncols - tn * g.TC));
+      pl_wait<1>();
+    } else {
+      pl_wait<0>();
+    }
+    __syncthreads();  // tile t (and the staged matrices) visible to all
+    pl_apply_tile<CT, SMAX>(T, Ms, g, tcv);
+    __syncthreads();
+    pl_store(out, T, g, goff, cb, tcv);
+    __syncthreads();  // buffer and bases free before they are refilled
+    pl_bases(cb, g, t + 2 * G);
+    __syncthreads();
+    buf ^= 1;
+  }
+}
+
+template <typename CT, int SMAX>
+__global__ void __launch_bounds__(PL_THREADS, 2)
+    plane_adjoint_kernel(const CT* __restrict__ psi_in, const CT* __restrict__ lam_out, CT* __restrict__ lam_in,
+                         const __grid_constant__ PlaneGeom g, const double2* __restrict__ mat, int mflags,
+                         double2* __restrict__ cpart, BatchArg bt) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  CT* MsH = reinterpret_cast<CT*>(smem);
+  int64_t* goff = reinterpret_cast<int64_t*>(smem + g.sm_goff);
+  int64_t* cb0 = reinterpret_cast<int64_t*>(smem + g.sm_cb);
+  CT* L = reinterpret_cast<CT*>(smem + g.sm_tile);
+  CT* P = L + (int64_t)g.TC * g.EP;
+  const int tid = threadIdx.x;
+  psi_in += blockIdx.z * bt.state_stride;
+  lam_out += blockIdx.z * bt.state_stride;
+  if (lam_in) lam_in += blockIdx.z * bt.state_stride;
+  mat += blockIdx.z * bt.mat_stride;
+  cpart += blockIdx.z * bt.part_stride + (int64_t)blockIdx.x * g.nent;
+  const int64_t GX = gridDim.x;
+  int64_t t = blockIdx.x;
+  pl_offsets(goff, g);
+  pl_bases(cb0, g, t);
+  pl_bases(cb0 + g.TC, g, t + GX);
+  __syncthreads();
+  if (t < g.ntiles) {
+    const int tcv = pl_cols(g.TC, g.ncols - t * g.TC);
+    pl_issue(lam_out, L, g, goff, cb0, tcv);
+    pl_issue(psi_in, P, g, goff, cb0, tcv);
+  }
+  if (lam_in) pl_stage(MsH, mat, g, mflags | MF_ADJOINT);
+
+  // C rows: thread -> (row r, column group cg); rows sorted by block size
+  const int G = g.G;
+  const bool activeA = tid < g.nrows * G;
+  const int r = activeA ? tid % g.nrows : 0;
+  const int cg = tid / g.nrows;
+  const int y = g.rows_y[r], u = g.rows_u[r];
+  const int s = g.s[y], base = g.base[y], step = g.step[y];
+  const int smax_warp = __reduce_max_sync(0xffffffffu, activeA ? s : 0);
+  CT acc[SMAX];
+#pragma unroll
+  for (int w = 0; w < SMAX; ++w) acc[w] = czero<CT>();
+
+  // bases of tile t at cb0 + cur*TC, of tile t + GX at the other half
+  int cur = 0;
+  for (; t < g.ntiles; t += GX) {
+    const int64_t tn = t + GX;
+    const int tcv = pl_cols(g.TC, g.ncols - t * g.TC);
+    int64_t* cb = cb0 + cur * g.TC;
+    int64_t* cbn = cb0 + (cur ^ 1) * g.TC;
+    pl_wait<0>();
+    __syncthreads();
+    if (activeA) {
+      for (int col = cg; col < tcv; col += G) {
+        const CT* lr = L + col * g.EP + base;
+        const CT* pr = P + col * g.EP + base;
+        const CT l = lr[u * step];
+#pragma unroll
+        for (int w = 0; w < SMAX; ++w) {
+          if (w >= smax_warp) break;
+          if (w < s) cfma_conj(acc[w], l, pr[w * step]);
+        }
+      }
+    }
+    __syncthreads();
+    const int tcn = tn < g.ntiles ? pl_cols(g.TC, g.ncols - tn * g.TC) : 0;
+    if (tn < g.ntiles) pl_issue(psi_in, P, g, goff, cbn, tcn);  // the psi tile is free
+    if (lam_in) {
+      pl_apply_tile<CT, SMAX>(L, MsH, g, tcv);
+      __syncthreads();
+      pl_store(lam_in, L, g, goff, cb, tcv);
+      __syncthreads();
+    }
+    if (tn < g.ntiles) pl_issue(lam_out, L, g, goff, cbn, tcn);
+    pl_bases(cb, g, tn + GX);  // tile t's bases are no longer read
+    cur ^= 1;
+  }
+  pl_wait<0>();
+  __syncthreads();
+  // partial C of this CTA (stored orientation)
+  if (G == 1) {
+    if (activeA) {
+      const int rv = g.rev[y];
+      const int a = rv ? s - 1 - u : u;
+      double2* dst = cpart + g.cout_off[y] + a * s;
+#pragma unroll
+      for (int w = 0; w < SMAX; ++w)
+        if (w < s) dst[rv ? s - 1 - w : w] = to_d(acc[w]);
+    }
+  } else {
+    // sum the G column groups of each row through shared memory (fixed order)
+    CT* red = L;
+    if (activeA) {
+#pragma unroll
+      for (int w = 0; w < SMAX; ++w)
+        if (w < s) red[((int64_t)cg * g.nrows + r) * g.D + w] = acc[w];
+    }
+    __syncthreads();
+    for (int rr = tid; rr < g.nrows; rr += PL_THREADS) {
+      const int yy = g.rows_y[rr], uu = g.rows_u[rr], ss = g.s[yy], rv = g.rev[yy];
+      const int a = rv ? ss - 1 - uu : uu;
+      for (int w = 0; w < ss; ++w) {
+        double2 sum = make_double2(0.0, 0.0);
+        for (int q = 0; q < G; ++q) {
+          const double2 v = to_d(red[((int64_t)q * g.nrows + rr) * g.D + w]);
+          sum.x += v.x;
+          sum.y += v.y;
+        }
+        cpart[g.cout_off[yy] + a * ss + (rv ? ss - 1 - w : w)] = sum;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, int adjoint, PlaneGeom* out) {
+  PlaneGeom g;
+  memset(&g, 0, sizeof(g));
+  const int esz = dtype == FOCK_C64 ? 8 : 16;
+  g.two = layout != LAYOUT_DENSE;
+  g.D = D;
+  g.E = g.two ? D * D : D;
+  if (g.two ? D > PL_MAX_D2 : D > PL_MAX_D1) return 0;
+  if (g.E > PL_THREADS && g.two) return 0;
+  g.EP = g.E | 1;
+  g.A = v.A; g.B = v.B; g.C = v.C; g.s1 = v.s1; g.s2 = v.s2; g.ncols = v.ncols;
+  g.c_inner = v.C >= 16 ? 1 : 0;
+  // the gate's axes are the innermost ones: column j's plane starts at j*E
+  g.flat = v.C == 1 && (!g.two || v.B == 1) ? 1 : 0;
+  g.emagic = (unsigned)(((1ull << 26) + g.E - 1) / g.E);
+  g.nblk = g.two ? 2 * D - 1 : 1;
+  int ms = 0, rows = 0;
+  for (int y = 0; y < g.nblk; ++y) {
+    if (!g.two) {
+      g.base[y] = 0; g.step[y] = 1; g.s[y] = (short)D; g.moff[y] = 0; g.rev[y] = 0; g.cout_off[y] = 0;
+    } else {
+      const int b = block_of_y(D, y);
+      const int s = blk_size(D, b);
+      g.s[y] = (short)s;
+      if (layout == LAYOUT_SUM) {
+        const int lo = blk_lo(D, 1, b);
+        g.base[y] = (short)(lo * D + (b - lo));
+        g.step[y] = (short)(D - 1);
+        g.moff[y] = blk_offset(D, b);
+        g.rev[y] = (unsigned char)(swap ? 1 : 0);
+        g.cout_off[y] = blk_offset(D, b);
+      } else {
+        const int delta = b - (D - 1);
+        const int lo = delta > 0 ? delta : 0;
+        g.base[y] = (short)(lo * D + (lo - delta));
+        g.step[y] = (short)(D + 1);
+        const int bs = swap ? 2 * D - 2 - b : b;
+        g.moff[y] = blk_offset(D, bs);
+        g.rev[y] = 0;
+        g.cout_off[y] = blk_offset(D, bs);
+      }
+    }
+    g.ms_off[y] = ms;
+    ms += g.s[y] * g.s[y];
+    for (int u = 0; u < g.s[y]; ++u) {
+      if (rows >= PL_THREADS) return 0;
+      g.rows_y[rows] = (unsigned char)y;
+      g.rows_u[rows] = (unsigned char)u;
+      ++rows;
+    }
+  }
+  g.ms_off[g.nblk] = ms;
+  g.ms_total = ms;
+  g.nent = ms;
+  g.nrows = rows;
+  g.G = std::max(1, PL_THREADS / rows);
+  // columns per tile: one warp of columns per block for two modes; enough
+  // column groups to give every warp a dense block otherwise
+  g.TC = g.two ? 32 : 256;
+  const size_t tile_cap = adjoint ? 96 * 1024 : 72 * 1024;  // both buffers
+  while (g.TC > 32 && (size_t)2 * g.TC * g.EP * esz > tile_cap) g.TC >>= 1;
+  g.ntiles = (g.ncols + g.TC - 1) / g.TC;
+  if (g.flat && (int64_t)g.TC * g.E >= (1 << 16)) return 0;
+  // warp items (block, column group), longest first onto the least loaded warp
+  const int ncg = g.TC / 32;
+  std::vector<std::pair<int, int>> items;  // (cost, item)
+  for (int y = 0; y < g.nblk; ++y)
+    for (int c = 0; c < ncg; ++c) items.push_back({g.s[y] * g.s[y], (y << 4) | c});
+  if ((int)items.size() > PL_MAX_ITEMS) return 0;
+  std::stable_sort(items.begin(), items.end(), [](const std::pair<int, int>& a, const std::pair<int, int>& b) {
+    return a.first > b.first;
+  });
+  std::vector<std::vector<int>> bins(PL_WARPS);
+  std::vector<long> load(PL_WARPS, 0);
+  for (auto& it : items) {
+    int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    bins[w].push_back(it.second);
+    load[w] += it.first;
+  }
+  int k = 0;
+  for (int w = 0; w < PL_WARPS; ++w) {
+    g.warp_start[w] = (short)k;
+    for (int it : bins[w]) g.items[k++] = (unsigned short)it;
+  }
+  g.warp_start[PL_WARPS] = (short)k;
+  // shared memory
+  g.sm_goff = (int)align16((size_t)ms * esz);
+  g.sm_cb = (int)align16((size_t)g.sm_goff + (size_t)g.E * 8);
+  g.sm_tile = (int)align16((size_t)g.sm_cb + (size_t)2 * g.TC * 8);
+  size_t tiles = (size_t)2 * g.TC * g.EP * esz;
+  if (adjoint) tiles = std::max(tiles, (size_t)PL_THREADS * D * esz);  // column-group reduction
+  g.smem = (int)(g.sm_tile + tiles);
+  if (g.smem > 200 * 1024) return 0;
+  *out = g;
+  return 1;
+}
+
+template <typename K>
+static int pl_resident(K k, int smem) {
+  int per_sm = 0;
+  if ((smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, PL_THREADS, smem) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  return per_sm;
+}
+
+template <typename CT, int SMAX>
+static int pl_resident_t(int adjoint, int smem) {
+  return adjoint ? pl_resident(plane_adjoint_kernel<CT, SMAX>, smem) : pl_resident(plane_apply_kernel<CT, SMAX>, smem);
+}
+
+template <typename CT>
+static int pl_resident_d(int adjoint, int D, int smem) {
+  switch (dmax_bucket(D)) {
+    case 4: return pl_resident_t<CT, 4>(adjoint, smem);
+    case 8: return pl_resident_t<CT, 8>(adjoint, smem);
+    case 12: return pl_resident_t<CT, 12>(adjoint, smem);
+    case 16: return pl_resident_t<CT, 16>(adjoint, smem);
+    case 20: return pl_resident_t<CT, 20>(adjoint, smem);
+    default: return pl_resident_t<CT, 24>(adjoint, smem);
+  }
+}
+
+int plane_preferred(int layout, const AxisView& v) {
+  // Two-mode ops on the innermost axis (C = 1): the block-per-CTA kernels
+  // read such planes with one sector per lane and re-fetch every sector once
+  // per block; the plane kernels read each plane once, coalesced.  Elsewhere
+  // the block kernels' direct register loads are already coalesced and
+  // cheaper.
+  return layout != LAYOUT_DENSE && v.C == 1;
+}
+
+int plane_grid(int dtype, const PlaneGeom& g, int adjoint, int nb) {
+  // resident CTAs per SM, cached per (device, kernel instance, shared memory)
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int, int>, int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    dev = -1;
+  }
+  const auto key = std::make_tuple(dev, dtype, dmax_bucket(g.D), adjoint, g.smem);
+  int per_sm = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) per_sm = it->second;
+  }
+  if (!per_sm) {
+    per_sm = dtype == FOCK_C64 ? pl_resident_d<float2>(adjoint, g.D, g.smem)
+                               : pl_resident_d<double2>(adjoint, g.D, g.smem);
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = per_sm;
+  }
+  int64_t grid = (int64_t)per_sm * fock_num_sms();
+  grid = (grid + nb - 1) / nb;
+  if (grid > g.ntiles) grid = g.ntiles;
+  if (grid < 1) grid = 1;
+  return (int)grid;
+}
+
+template <typename CT, int SMAX>
+static int pl_launch_t(int adjoint, const void* a, const void* b, void* c, const PlaneGeom& g, int grid,
+                       const double2* mat, int mflags, double2* cpart, cudaStream_t st, const BatchArg& bt) {
+  if (bt.nb < 1 || bt.nb > 65535) return fock_set_error(FOCK_ERR_INVALID, "batch of %d circuits", bt.nb);
+  dim3 gr(grid, 1, bt.nb);
+  if (!adjoint) {
+    auto k = plane_apply_kernel<CT, SMAX>;
+    if (g.smem > 48 * 1024) FOCK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, g.smem));
+    k<<<gr, PL_THREADS, g.smem, st>>>((const CT*)a, (CT*)c, g, mat, mflags, bt);
+    FOCK_LAUNCH_CHECK("plane_apply_kernel");
+  } else {
+    auto k = plane_adjoint_kernel<CT, SMAX>;
+    if (g.smem > 48 * 1024) FOCK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, g.smem));
+    k<<<gr, PL_THREADS, g.smem, st>>>((const CT*)a, (const CT*)b, (CT*)c, g, mat, mflags, cpart, bt);
+    FOCK_LAUNCH_CHECK("plane_adjoint_kernel");
+  }
+  return FOCK_OK;
+}
+
+template <typename CT>
+static int pl_launch_d(int adjoint, const void* a, const void* b, void* c, const PlaneGeom& g, int grid,
+                       const double2* mat, int mflags, double2* cpart, cudaStream_t st, const BatchArg& bt) {
+  switch (dmax_bucket(g.D)) {
+    case 4: return pl_launch_t<CT, 4>(adjoint, a, b, c, g, grid, mat, mflags, cpart, st, bt);
+    case 8: return pl_launch_t<CT, 8>(adjoint, a, b, c, g, grid, mat, mflags, cpart, st, bt);
+    case 12: return pl_launch_t<CT, 12>(adjoint, a, b, c, g, grid, mat, mflags, cpart, st, bt);
+    case 16: return pl_launch_t<CT, 16>(adjoint, a, b, c, g, grid, mat, mflags, cpart, st, bt);
+    case 20: return pl_launch_t<CT, 20>(adjoint, a, b, c, g, grid, mat, mflags, cpart, st, bt);
+    default: return pl_launch_t<CT, 24>(adjoint, a, b, c, g, grid, mat, mflags, cpart, st, bt);
+  }
+}
+
+int launch_plane_apply(int dtype, const void* in, void* out, const PlaneGeom& g, int grid, const double2* mat,
+                       int mflags, cudaStream_t st, const BatchArg& bt) {
+  if (g.ncols <= 0) return FOCK_OK;
+  if (dtype == FOCK_C64) return pl_launch_d<float2>(0, in, nullptr, out, g, grid, mat, mflags, nullptr, st, bt);
+  return pl_launch_d<double2>(0, in, nullptr, out, g, grid, mat, mflags, nullptr, st, bt);
+}
+
+int launch_plane_adjoint(int dtype, const void* psi_in, const void* lam_out, void* lam_in, const PlaneGeom& g,
+                         int grid, const double2* mat, int mflags, double2* cpart, cudaStream_t st,
+                         const BatchArg& bt) {
+  if (dtype == FOCK_C64)
+    return pl_launch_d<float2>(1, psi_in, lam_out, lam_in, g, grid, mat, mflags, cpart, st, bt);
+  return pl_launch_d<double2>(1, psi_in, lam_out, lam_in, g, grid, mat, mflags, cpart, st, bt);
+}

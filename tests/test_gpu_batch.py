@@ -1,0 +1,36 @@
+"""Heterogeneous circuit batches (rows Q1/Q2): circuits of different modes,
+cutoffs and depths grouped by structure, each group a batched compiled
+circuit; every circuit's loss and gradient against the oracle."""
+import numpy as np
+import pytest
+
+from oracle import fock_oracle as fo
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_heterogeneous_batch_matches_oracle(cuda, dtype):
+    import torch
+    from strawberryfields_gb300.batch import CircuitBatch, random_qnn_batch
+    from strawberryfields_gb300.qnn import target_state
+
+    circuits, params = random_qnn_batch(14, seed=3, modes=(2, 3), cutoffs=(4, 6), depths=(1, 2))
+    tdt = torch.complex128 if dtype == "complex128" else torch.complex64
+    # a tiny checkpoint threshold forces the checkpointed sweep on some groups
+    cb = CircuitBatch(circuits, dtype=tdt, streams=3, checkpoint_bytes=20_000)
+    assert cb.stats()["groups"] < len(circuits) or len(circuits) <= 1
+    targets = {}
+    for nm, D, _, _ in circuits:
+        targets[(nm, D)] = torch.as_tensor(target_state(nm, D, 2, seed=nm * 100 + D), device="cuda")
+    pt = [torch.tensor(p, device="cuda") for p in params]
+    losses, grads = cb.value_and_grad(pt, targets)
+    torch.cuda.synchronize()
+    for i, (nm, D, gates, npar) in enumerate(circuits):
+        t = targets[(nm, D)].cpu().numpy()
+        psi = fo.run_gates(gates, params[i], nm, D)[-1]
+        s = np.vdot(t, psi)
+        assert abs(losses[i].item() - (1 - abs(s) ** 2)) < (1e-12 if dtype == "complex128" else 1e-5)
+        ref = fo.adjoint_grads(gates, params[i], nm, D, -2 * s * t)
+        rel = np.linalg.norm(grads[i].cpu().numpy() - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert rel < (1e-10 if dtype == "complex128" else 1e-5), (i, rel)

@@ -192,3 +192,25 @@ def test_batched_circuits_match_individual_runs(cuda, dtype):
         ref = fo.adjoint_grads(gates, P[b], N, D, _loss_grad(ref_states[-1], t)[1])
         rel = np.linalg.norm(p.grad[b].cpu().numpy() - ref) / np.linalg.norm(ref)
         assert rel < (1e-10 if dtype == "complex128" else 1e-5), (b, rel)
+
+
+@pytest.mark.parametrize("k", [2, 3, 7])
+def test_checkpointed_adjoint_matches_stored(cuda, k):
+    """Keeping every k-th state and recomputing segments gives the same gradient."""
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+    from strawberryfields_gb300.qnn import qnn_gates, qnn_params, target_state
+
+    N, D = 3, 6
+    gates, npar = qnn_gates(N, 2)
+    params = qnn_params(gates, npar, seed=8)
+    t = torch.as_tensor(target_state(N, D, 3, seed=9), device="cuda")
+    out = []
+    for kk in (1, k):
+        circ = CompiledCircuit(N, D, gates, npar, dtype=torch.complex128, checkpoint=kk)
+        p = torch.tensor(params, device="cuda", requires_grad=True)
+        psi = circ(p)
+        (1 - torch.abs(torch.sum(t.conj() * psi)) ** 2).backward()
+        out.append((psi.detach().cpu().numpy(), p.grad.cpu().numpy()))
+    assert np.abs(out[0][0] - out[1][0]).max() < 1e-13
+    assert np.abs(out[0][1] - out[1][1]).max() < 1e-12
