@@ -230,6 +230,8 @@ __global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)
   CT* MsH = reinterpret_cast<CT*>(smem_raw);
   CT* lam_s = MsH + ((s * s + 1) & ~1);
   CT* psi_s = lam_s + rows * (TILE + 1);
+  pdl_wait();
+  pdl_launch_dependents();
   AdjDispatch<CT, 1, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s, g, mypart,
                                       xrank, gxb, write_lam);
 }
@@ -321,6 +323,8 @@ AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout) {
 
 __global__ void reduce_sched_kernel(const double2* __restrict__ cpart, AdjSched sc, int D, int layout,
                                     double2* __restrict__ cout, int64_t part_stride, int64_t out_stride) {
+  pdl_wait();
+  pdl_launch_dependents();
   const int lane = threadIdx.x & 31;
   const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   cpart += blockIdx.y * part_stride;
@@ -357,12 +361,11 @@ __global__ void reduce_sched_kernel(const double2* __restrict__ cpart, AdjSched 
 }
 
 int launch_reduce_sched(const double2* cpart, const AdjSched& sc, int D, int layout, double2* cout, cudaStream_t st,
-                        int nb, int64_t part_stride, int64_t out_stride) {
+                        int nb, int64_t part_stride, int64_t out_stride, int pdl) {
   const int64_t nent = layout == LAYOUT_DENSE ? (int64_t)D * D : blk_total(D);
   const int64_t blocks = (nent * 32 + 255) / 256;
-  reduce_sched_kernel<<<dim3((unsigned)blocks, nb), 256, 0, st>>>(cpart, sc, D, layout, cout, part_stride,
-                                                                  out_stride);
-  FOCK_LAUNCH_CHECK("reduce_sched_kernel");
+  FOCK_CUDA_TRY(launch_kernel(reduce_sched_kernel, dim3((unsigned)blocks, nb), dim3(256), 0, st, pdl, cpart, sc, D,
+                               layout, cout, part_stride, out_stride));
   return FOCK_OK;
 }
 
@@ -374,9 +377,8 @@ static int launch_adj_t(const void* psi_in, const void* lam_out, void* lam_in, c
   auto k = adjoint_block_kernel<CT, TILE, DMAX>;
   if (sm > 48 * 1024) FOCK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   dim3 grid(sc.total, 1, bt.nb);
-  k<<<grid, TILE, sm, st>>>((const CT*)psi_in, (const CT*)lam_out, (CT*)lam_in, v, D, layout, mat, mflags, cpart, sc,
-                            lam_in != nullptr, bt);
-  FOCK_LAUNCH_CHECK("adjoint_block_kernel");
+  FOCK_CUDA_TRY(launch_kernel(k, grid, dim3(TILE), sm, st, bt.pdl, (const CT*)psi_in, (const CT*)lam_out, (CT*)lam_in,
+                               v, D, layout, mat, mflags, cpart, sc, (int)(lam_in != nullptr), bt));
   return FOCK_OK;
 }
 
@@ -407,6 +409,8 @@ int launch_adjoint_partials(int dtype, const void* psi_in, const void* lam_out, 
 // cout[e] = sum_x cpart[x][e]  (one warp per entry, fixed summation order)
 __global__ void reduce_partials_kernel(const double2* __restrict__ cpart, int gx, int64_t nent,
                                        double2* __restrict__ cout, int64_t part_stride, int64_t out_stride) {
+  pdl_wait();
+  pdl_launch_dependents();
   const int lane = threadIdx.x & 31;
   // blockIdx.y: circuit of a batch
   cpart += blockIdx.y * part_stride;
@@ -428,12 +432,11 @@ __global__ void reduce_partials_kernel(const double2* __restrict__ cpart, int gx
 }
 
 int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* cout, cudaStream_t st, int nb,
-                           int64_t part_stride, int64_t out_stride) {
+                           int64_t part_stride, int64_t out_stride, int pdl) {
   const int64_t threads = nent * 32;
   const int64_t blocks = (threads + 255) / 256;
-  reduce_partials_kernel<<<dim3((unsigned)blocks, nb), 256, 0, st>>>(cpart, gx, nent, cout, part_stride,
-                                                                      out_stride);
-  FOCK_LAUNCH_CHECK("reduce_partials_kernel");
+  FOCK_CUDA_TRY(launch_kernel(reduce_partials_kernel, dim3((unsigned)blocks, nb), dim3(256), 0, st, pdl, cpart, gx, nent,
+                               cout, part_stride, out_stride));
   return FOCK_OK;
 }
 

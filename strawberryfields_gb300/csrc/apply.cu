@@ -119,6 +119,8 @@ __global__ void __launch_bounds__(APPLY_THREADS, ApplyMinBlocks<DMAX>::value) ap
   const int b = layout == LAYOUT_DENSE ? 0 : block_of_y(D, blockIdx.y);
   const BlockGeom g = block_geom(v, D, layout, b, (mflags & MF_SWAP) ? 1 : 0);
   const int64_t j0 = (int64_t)blockIdx.x * (APPLY_THREADS * APPLY_COLS) + threadIdx.x;
+  pdl_wait();
+  pdl_launch_dependents();
   ApplyDispatch<CT, 1, DMAX>::run(in, out, v, D, Ms, mat, mflags, g, j0);
 }
 
@@ -133,8 +135,8 @@ static int launch_apply_t(const void* in, void* out, const AxisView& v, int D, i
   const size_t sm = (size_t)D * D * sizeof(CT);
   auto k = apply_block_kernel<CT, DMAX>;
   if (sm > 48 * 1024) FOCK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-  k<<<grid, APPLY_THREADS, sm, st>>>((const CT*)in, (CT*)out, v, D, layout, mat, mflags, bt);
-  FOCK_LAUNCH_CHECK("apply_block_kernel");
+  FOCK_CUDA_TRY(launch_kernel(k, grid, dim3(APPLY_THREADS), sm, st, bt.pdl, (const CT*)in, (CT*)out, v, D, layout,
+                               mat, mflags, bt));
   return FOCK_OK;
 }
 

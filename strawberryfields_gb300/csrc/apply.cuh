@@ -99,7 +99,36 @@ struct BatchArg {
   int64_t state_stride = 0;
   int64_t mat_stride = 0;
   int64_t part_stride = 0;
+  int pdl = 0;  // host only: launch with programmatic dependent launch
 };
+
+// Programmatic dependent launch.  A kernel launched with the attribute may
+// start while its stream predecessor is still running: it does its index
+// set-up, then waits in pdl_wait() until the predecessor has completed and
+// its writes are visible, before it reads or writes any state, and calls
+// pdl_launch_dependents() so that its own successor can be launched once all
+// of its CTAs are resident.  Without the attribute both are no-ops.  Because
+// every kernel waits for its predecessor's completion, all earlier kernels
+// of the stream have completed when the wait returns.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() {
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_kernel(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, int pdl,
+                                 Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
 
 // Apply a built matrix (FP64 in `mat`, layout LAYOUT_*) on a view: out = M in.
 int launch_apply(int dtype, const void* in, void* out, const AxisView& v, int D, int layout,
@@ -128,10 +157,10 @@ int launch_adjoint_partials(int dtype, const void* psi_in, const void* lam_out, 
                             const AxisView& v, int D, int layout, const double2* mat, int mflags,
                             double2* cpart, const AdjSched& sc, cudaStream_t st, const BatchArg& bt = BatchArg());
 int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* cout, cudaStream_t st, int nb = 1,
-                           int64_t part_stride = 0, int64_t out_stride = 0);
+                           int64_t part_stride = 0, int64_t out_stride = 0, int pdl = 0);
 // sum the partials of a schedule into `cout` (stored orientation, layout entries)
 int launch_reduce_sched(const double2* cpart, const AdjSched& sc, int D, int layout, double2* cout, cudaStream_t st,
-                        int nb = 1, int64_t part_stride = 0, int64_t out_stride = 0);
+                        int nb = 1, int64_t part_stride = 0, int64_t out_stride = 0, int pdl = 0);
 
 // Plane-tile kernels (plane.cu): a persistent CTA stages TC columns' whole
 // planes (D elements for one mode, D x D for two) in shared memory and applies

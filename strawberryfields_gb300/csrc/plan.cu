@@ -516,6 +516,10 @@ extern "C" int fock_plan_forward(fock_plan* P, const double* params, const void*
   for (int k = 0; k < n_ops; ++k) {
     void* dst = (char*)states + out_slot(k, n_ops, store_every) * c.sb;
     if (P->timing && (rc = record_event(P->ev_fwd[k], st))) return rc;
+    // the first op follows the matrix build in plain stream order; later ops
+    // overlap their launch with the previous op's tail (not across the
+    // timing events)
+    c.bt.pdl = k > 0 && !P->timing;
     if ((rc = apply_op(c, k, cur, dst))) return rc;
     cur = dst;
   }
@@ -551,6 +555,10 @@ extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void
     P->bwd_recorded = 0;
   }
   const int nseg = K == 1 ? 1 : (n_ops + K - 1) / K;
+  // programmatic dependent launch for every sweep kernel but the first one
+  // after the matrix build (and none around timing events)
+  const int pdl = !P->timing;
+  c.bt.pdl = 0;
   for (int sgi = nseg - 1; sgi >= 0; --sgi) {
     const int s0 = K == 1 ? 0 : sgi * K;
     const int e = K == 1 ? n_ops : std::min(s0 + K, n_ops);
@@ -562,6 +570,7 @@ extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void
       for (int j = s0; j < e - 1; ++j) {
         void* dst = (char*)seg + (int64_t)(j - s0) * c.sb;
         if ((rc = apply_op(c, j, cur, dst))) return rc;
+        c.bt.pdl = pdl;
         cur = dst;
       }
     }
@@ -577,15 +586,16 @@ extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void
                                   op.swap ? MF_SWAP : 0, cpart, st, c.bt);
         if (rc) return rc;
         rc = launch_reduce_partials(cpart, op.grid_adj, op.nent, cout, st, P->batch, P->cpart_entries,
-                                    P->carena_entries);
+                                    P->carena_entries, pdl);
       } else {
         rc = launch_adjoint_partials(P->dtype, psi_in, lam, other, op.view, P->D, op.layout, c.arena + op.m_off,
                                      op.swap ? MF_SWAP : 0, cpart, op.sched, st, c.bt);
         if (rc) return rc;
         rc = launch_reduce_sched(cpart, op.sched, P->D, op.layout, cout, st, P->batch, P->cpart_entries,
-                                 P->carena_entries);
+                                 P->carena_entries, pdl);
       }
       if (rc) return rc;
+      c.bt.pdl = pdl;
       void* t = lam;
       lam = other;
       other = t;

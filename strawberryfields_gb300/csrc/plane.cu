@@ -216,6 +216,8 @@ __global__ void __launch_bounds__(PL_THREADS, 2)
   pl_bases(cb0, g, t);
   pl_bases(cb0 + g.TC, g, t + G);
   __syncthreads();
+  pdl_wait();
+  pdl_launch_dependents();
   if (t < g.ntiles) pl_issue(in, T0, g, goff, cb0, pl_cols(g.TC, g.ncols - t * g.TC));
   pl_stage(Ms, mat, g, mflags);  // overlaps the first tile's copies
   int buf = 0;
@@ -265,6 +267,8 @@ __global__ void __launch_bounds__(PL_THREADS, 2)
   pl_bases(cb0, g, t);
   pl_bases(cb0 + g.TC, g, t + GX);
   __syncthreads();
+  pdl_wait();
+  pdl_launch_dependents();
   if (t < g.ntiles) {
     const int tcv = pl_cols(g.TC, g.ncols - t * g.TC);
     pl_issue(lam_out, L, g, goff, cb0, tcv);
@@ -531,13 +535,12 @@ static int pl_launch_t(int adjoint, const void* a, const void* b, void* c, const
   if (!adjoint) {
     auto k = plane_apply_kernel<CT, SMAX>;
     if (g.smem > 48 * 1024) FOCK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, g.smem));
-    k<<<gr, PL_THREADS, g.smem, st>>>((const CT*)a, (CT*)c, g, mat, mflags, bt);
-    FOCK_LAUNCH_CHECK("plane_apply_kernel");
+    FOCK_CUDA_TRY(launch_kernel(k, gr, dim3(PL_THREADS), g.smem, st, bt.pdl, (const CT*)a, (CT*)c, g, mat, mflags, bt));
   } else {
     auto k = plane_adjoint_kernel<CT, SMAX>;
     if (g.smem > 48 * 1024) FOCK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, g.smem));
-    k<<<gr, PL_THREADS, g.smem, st>>>((const CT*)a, (const CT*)b, (CT*)c, g, mat, mflags, cpart, bt);
-    FOCK_LAUNCH_CHECK("plane_adjoint_kernel");
+    FOCK_CUDA_TRY(launch_kernel(k, gr, dim3(PL_THREADS), g.smem, st, bt.pdl, (const CT*)a, (const CT*)b, (CT*)c, g, mat,
+                                 mflags, cpart, bt));
   }
   return FOCK_OK;
 }
