@@ -402,9 +402,9 @@ def single_gate_case(args):
 
     dev = torch.device("cuda", 0)
     lib = _lib.load()
-    N, D = 7, 12
-    cases = {"dense1_inner": [(4, 2, -1, 0)], "dense1_last": [(4, 6, -1, 0)],
-             "block2_inner": [(5, 2, 3, 0)], "block2_last": [(5, 5, 6, 0)]}
+    N, D = args.modes, 12
+    cases = {"dense1_inner": [(4, 2, -1, 0)], "dense1_last": [(4, N - 1, -1, 0)],
+             "block2_inner": [(5, 2, 3, 0)], "block2_last": [(5, N - 2, N - 1, 0)]}
     if args.only:
         cases = {k: v for k, v in cases.items() if k in args.only.split(",")}
     rng = np.random.default_rng(0)
@@ -506,6 +506,7 @@ def main():
     ap.add_argument("--case", default="gradient", choices=["gradient", "single-gate", "batched"])
     ap.add_argument("--circuits", type=int, default=4096)
     ap.add_argument("--only", default="", help="single-gate case: comma-separated subset of the kernels")
+    ap.add_argument("--modes", type=int, default=7, help="single-gate case: modes of the cutoff-12 ket")
     ap.add_argument("--eager", action="store_true", help="no CUDA graph capture")
     args = ap.parse_args()
     if args.case == "single-gate":

@@ -208,6 +208,20 @@ int fock_plan_backward(fock_plan* plan, const double* params, const void* state_
 int fock_plan_enable_timing(fock_plan* plan, int enable);
 int fock_plan_op_times(fock_plan* plan, float* fwd_ms, float* bwd_ms);
 
+/* Persistent sweeps.  A single-circuit complex64 plan whose state is at most
+ * FOCK_GB300_SWEEP_MAX_BYTES bytes (read at plan creation; default 0 = off,
+ * since per-op launches measured faster on GB300) runs a forward
+ * sweep with store_every 0 or 1, and a backward sweep with store_every 1, as
+ * one cooperative launch that walks every op with a grid barrier between ops
+ * (no per-op launch).  Per-op timing and checkpointed sweeps use the per-op
+ * launches.  `grids` (2 ints, or null) receives the CTAs of the persistent
+ * forward and backward launches (0 when the plan uses per-op launches); `error` is
+ * nonzero when a grid barrier of the last persistent sweep on `workspace`
+ * gave up waiting (the outputs are then invalid).  Synchronous: call after
+ * the sweep's stream has been synchronised.  No reference counterpart (the
+ * reference applies one gate per Python call, fockbackend/circuit.py). */
+int fock_plan_sweep_status(const fock_plan* plan, const void* workspace, int* grids, int* error);
+
 #ifdef __cplusplus
 }
 #endif

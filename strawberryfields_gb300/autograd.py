@@ -179,6 +179,18 @@ class CompiledCircuit:
                 "fock_plan_backward")
         return grads, lam
 
+    def sweep_status(self):
+        """(persistent, error): whether this plan runs its sweeps as single
+        persistent launches, and whether a grid barrier of the last such sweep
+        gave up (outputs invalid).  Synchronises the device."""
+        torch.cuda.synchronize(self.device)
+        grids, err = (ctypes.c_int * 2)(), ctypes.c_int()
+        ws = self._ws_buf.data_ptr() if self._ws_buf is not None else None
+        L.check(L.load().fock_plan_sweep_status(self._plan, ws, grids, ctypes.byref(err) if ws else None),
+                "fock_plan_sweep_status")
+        self.sweep_grids = (grids[0], grids[1])
+        return grids[0] > 0, int(err.value)
+
     def __call__(self, params, state_in=None):
         """Final state as a differentiable function of ``params``."""
         return _CircuitFunction.apply(params, self, state_in)

@@ -21,188 +21,9 @@
 // blocks first; kernels are compiled per cutoff bucket.
 // Partial C's of each CTA go to `cpart` ([gridDim.x][entries], FP64); a
 // separate deterministic reduction sums them.
-#include "apply.cuh"
+#include "block_body.cuh"
 
 #include <string.h>
-
-template <int S> struct RRof { static const int value = (S + 3) / 4; };
-
-// Asynchronous global -> shared copies (cp.async): the tile lands in shared
-// memory without passing through registers; invalid columns are zero-filled.
-__device__ __forceinline__ void cp_async_elem(float2* dst, const float2* src, bool valid) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(src), "r"(valid ? 8 : 0));
-}
-__device__ __forceinline__ void cp_async_elem(double2* dst, const double2* src, bool valid) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(src), "r"(valid ? 16 : 0));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-template <typename CT, int S, int TILE>
-__device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, const CT* __restrict__ lam_out,
-                                             CT* __restrict__ lam_in, const AxisView& v, int D, CT* MsH,
-                                             const double2* __restrict__ mat, int mflags, CT* lam_s, CT* psi_s,
-                                             const BlockGeom& g, double2* __restrict__ mypart, int xrank, int gxb,
-                                             int write_lam) {
-  constexpr int RR = RRof<S>::value;
-  constexpr int NG = TILE / 16;
-  constexpr int LD = TILE + 1;  // padded row stride (elements)
-  const int tid = threadIdx.x;
-  const int owner = tid / NG, grp = tid - owner * NG;
-  const int ro = owner >> 2, co = owner & 3;
-  CT acc[RR][RR];
-#pragma unroll
-  for (int r = 0; r < RR; ++r)
-#pragma unroll
-    for (int c = 0; c < RR; ++c) acc[r][c] = czero<CT>();
-
-  const int64_t ntiles = (v.ncols + TILE - 1) / TILE;
-  auto issue = [&](int64_t t) {
-    const int64_t j = t * TILE + tid;
-    const bool valid = j < v.ncols;
-    const int64_t base = valid ? col_base(v, j, D) + g.boff : 0;
-#pragma unroll
-    for (int u = 0; u < S; ++u) {
-      const int64_t off = valid ? base + u * g.step : 0;
-      cp_async_elem(&lam_s[u * LD + tid], lam_out + off, valid);
-      cp_async_elem(&psi_s[u * LD + tid], psi_in + off, valid);
-    }
-    cp_async_commit();
-  };
-  // the first tile's copies are in flight while the block is staged
-  if (xrank < ntiles) issue(xrank);
-  if (write_lam) stage_block(MsH, mat, g, mflags | MF_ADJOINT);
-  // padding rows s..4*RR-1 stay zero
-  for (int e = tid; e < (4 * RR - S) * LD; e += TILE) {
-    lam_s[S * LD + e] = czero<CT>();
-    psi_s[S * LD + e] = czero<CT>();
-  }
-  __syncthreads();
-  for (int64_t t = xrank; t < ntiles; t += gxb) {
-    cp_async_wait_all();  // this thread's column has landed
-    const int64_t j = t * TILE + tid;
-    if (write_lam && j < v.ncols) {
-      // each thread reads back only its own column: no barrier needed here
-      const int64_t base = col_base(v, j, D) + g.boff;
-      CT lam[S];
-#pragma unroll
-      for (int u = 0; u < S; ++u) lam[u] = lam_s[u * LD + tid];
-#pragma unroll
-      for (int w = 0; w < S; ++w) {
-        CT a = czero<CT>();
-#pragma unroll
-        for (int u = 0; u < S; ++u) cfma(a, MsH[w * S + u], lam[u]);
-        lam_in[base + w * g.step] = a;
-      }
-    }
-    __syncthreads();  // every thread's column of tile t has landed
-#pragma unroll 2
-    for (int step = 0; step < TILE / NG; ++step) {
-      const int col = step * NG + grp;
-      CT lv[RR], pv[RR];
-#pragma unroll
-      for (int r = 0; r < RR; ++r) lv[r] = lam_s[(ro * RR + r) * LD + col];
-#pragma unroll
-      for (int c = 0; c < RR; ++c) pv[c] = psi_s[(co * RR + c) * LD + col];
-#pragma unroll
-      for (int r = 0; r < RR; ++r)
-#pragma unroll
-        for (int c = 0; c < RR; ++c) cfma_conj(acc[r][c], lv[r], pv[c]);
-    }
-    __syncthreads();  // the tile buffers are free for the next tile
-    if (t + gxb < ntiles) issue(t + gxb);
-  }
-  // reduce over the NG groups of each owner (adjacent lanes)
-#pragma unroll
-  for (int off = NG / 2; off > 0; off >>= 1) {
-#pragma unroll
-    for (int r = 0; r < RR; ++r)
-#pragma unroll
-      for (int c = 0; c < RR; ++c) {
-        acc[r][c].x += __shfl_xor_sync(0xffffffffu, acc[r][c].x, off);
-        acc[r][c].y += __shfl_xor_sync(0xffffffffu, acc[r][c].y, off);
-      }
-  }
-  if (grp == 0) {
-#pragma unroll
-    for (int r = 0; r < RR; ++r)
-#pragma unroll
-      for (int c = 0; c < RR; ++c) {
-        int u = ro * RR + r, w = co * RR + c;
-        if (u < S && w < S) {
-          int a = g.rev ? S - 1 - u : u;
-          int b = g.rev ? S - 1 - w : w;
-          mypart[a * S + b] = to_d(acc[r][c]);
-        }
-      }
-  }
-}
-
-template <typename CT, int TILE>
-__device__ void adjoint_generic(const CT* __restrict__ psi_in, const CT* __restrict__ lam_out,
-                                CT* __restrict__ lam_in, const AxisView& v, int D, CT* MsH,
-                                const double2* __restrict__ mat, int mflags, const BlockGeom& g,
-                                double2* __restrict__ mypart, int xrank, int gxb, int write_lam) {
-  if (write_lam) stage_block(MsH, mat, g, mflags | MF_ADJOINT);
-  __syncthreads();
-  // large blocks (beyond the unrolled buckets): thread per C entry over this
-  // CTA's share of the columns, then lam_in per column
-  const int S = g.s;
-  const int64_t per = (v.ncols + gxb - 1) / gxb;
-  int64_t j0 = xrank * per, j1 = j0 + per;
-  if (j1 > v.ncols) j1 = v.ncols;
-  for (int e = threadIdx.x; e < S * S; e += blockDim.x) {
-    int u = e / S, w = e - u * S;
-    double2 a = make_double2(0.0, 0.0);
-    for (int64_t j = j0; j < j1; ++j) {
-      const int64_t base = col_base(v, j, D) + g.boff;
-      double2 ld = to_d(lam_out[base + u * g.step]), pd = to_d(psi_in[base + w * g.step]);
-      cfma_conj(a, ld, pd);
-    }
-    int aa = g.rev ? S - 1 - u : u, bb = g.rev ? S - 1 - w : w;
-    mypart[aa * S + bb] = a;
-  }
-  if (!write_lam) return;
-  for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
-    const int64_t base = col_base(v, j, D) + g.boff;
-    for (int w = 0; w < S; ++w) {
-      CT a = czero<CT>();
-      for (int u = 0; u < S; ++u) cfma(a, MsH[w * S + u], lam_out[base + u * g.step]);
-      lam_in[base + w * g.step] = a;
-    }
-  }
-}
-
-template <typename CT, int S, int DMAX, int TILE>
-struct AdjDispatch {
-  __device__ __forceinline__ static void run(const CT* psi_in, const CT* lam_out, CT* lam_in, const AxisView& v,
-                                             int D, CT* MsH, const double2* mat, int mflags, CT* lam_s, CT* psi_s,
-                                             const BlockGeom& g, double2* mypart, int xrank, int gxb,
-                                             int write_lam) {
-    if (g.s == S)
-      adjoint_body<CT, S, TILE>(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s, g, mypart, xrank,
-                                gxb, write_lam);
-    else
-      AdjDispatch<CT, S + 1, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s, g,
-                                              mypart, xrank, gxb, write_lam);
-  }
-};
-template <typename CT, int DMAX, int TILE>
-struct AdjDispatch<CT, DMAX + 1, DMAX, TILE> {
-  __device__ __forceinline__ static void run(const CT* psi_in, const CT* lam_out, CT* lam_in, const AxisView& v,
-                                             int D, CT* MsH, const double2* mat, int mflags, CT*, CT*,
-                                             const BlockGeom& g, double2* mypart, int xrank, int gxb,
-                                             int write_lam) {
-    adjoint_generic<CT, TILE>(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, g, mypart, xrank, gxb, write_lam);
-  }
-};
-
-// 3 resident CTAs (24 warps) per SM for complex64 cutoffs up to 12
-template <typename CT, int DMAX> struct AdjMinBlocks {
-  static const int value = (sizeof(CT) == 8 && DMAX > 0 && DMAX <= 12) ? 3 : 1;
-};
 
 template <typename CT, int TILE, int DMAX>
 __global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)

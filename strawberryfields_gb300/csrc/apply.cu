@@ -40,72 +40,7 @@ AxisView make_view2(int naxes, int D, int ax1, int ax2) {
   return v;
 }
 
-#define APPLY_THREADS 256
-#define APPLY_COLS 1
-
-// The column's loads are issued before the block is staged in shared memory,
-// so the two global round trips overlap.
-template <typename CT, int S>
-__device__ __forceinline__ void apply_cols(const CT* __restrict__ in, CT* __restrict__ out,
-                                           const AxisView& v, int D, CT* Ms, const double2* mat, int mflags,
-                                           const BlockGeom& g, int64_t j0) {
-  const bool valid = j0 < v.ncols;
-  const int64_t b0 = valid ? col_base(v, j0, D) + g.boff : 0;
-  CT x0[S];
-  if (valid) {
-#pragma unroll
-    for (int u = 0; u < S; ++u) x0[u] = __ldg(in + b0 + u * g.step);
-  }
-  stage_block(Ms, mat, g, mflags);
-  __syncthreads();
-  if (!valid) return;
-#pragma unroll
-  for (int w = 0; w < S; ++w) {
-    CT a0 = czero<CT>();
-#pragma unroll
-    for (int u = 0; u < S; ++u) cfma(a0, Ms[w * S + u], x0[u]);
-    out[b0 + w * g.step] = a0;
-  }
-}
-
-template <typename CT>
-__device__ void apply_cols_generic(const CT* __restrict__ in, CT* __restrict__ out, const AxisView& v,
-                                   int D, CT* Ms, const double2* mat, int mflags, const BlockGeom& g,
-                                   int64_t j0) {
-  stage_block(Ms, mat, g, mflags);
-  __syncthreads();
-  for (int k = 0; k < APPLY_COLS; ++k) {
-    const int64_t j = j0 + k * APPLY_THREADS;
-    if (j >= v.ncols) break;
-    const int64_t base = col_base(v, j, D) + g.boff;
-    const int S = g.s;
-    for (int w = 0; w < S; ++w) {
-      CT acc = czero<CT>();
-      for (int u = 0; u < S; ++u) cfma(acc, Ms[w * S + u], in[base + u * g.step]);
-      out[base + w * g.step] = acc;
-    }
-  }
-}
-
-// s == S ? run the unrolled body : try S + 1 (up to DMAX)
-template <typename CT, int S, int DMAX>
-struct ApplyDispatch {
-  __device__ __forceinline__ static void run(const CT* in, CT* out, const AxisView& v, int D, CT* Ms,
-                                             const double2* mat, int mflags, const BlockGeom& g, int64_t j0) {
-    if (g.s == S) apply_cols<CT, S>(in, out, v, D, Ms, mat, mflags, g, j0);
-    else ApplyDispatch<CT, S + 1, DMAX>::run(in, out, v, D, Ms, mat, mflags, g, j0);
-  }
-};
-template <typename CT, int DMAX>
-struct ApplyDispatch<CT, DMAX + 1, DMAX> {
-  __device__ __forceinline__ static void run(const CT* in, CT* out, const AxisView& v, int D, CT* Ms,
-                                             const double2* mat, int mflags, const BlockGeom& g, int64_t j0) {
-    apply_cols_generic<CT>(in, out, v, D, Ms, mat, mflags, g, j0);
-  }
-};
-
-// 4 resident CTAs (32 warps) per SM for cutoffs up to 12, 2 beyond
-template <int DMAX> struct ApplyMinBlocks { static const int value = (DMAX > 0 && DMAX <= 12) ? 4 : 2; };
+#include "block_body.cuh"
 
 template <typename CT, int DMAX>
 __global__ void __launch_bounds__(APPLY_THREADS, ApplyMinBlocks<DMAX>::value) apply_block_kernel(

@@ -203,6 +203,51 @@ int launch_plane_adjoint(int dtype, const void* psi_in, const void* lam_out, voi
                          int grid, const double2* mat, int mflags, double2* cpart, cudaStream_t st,
                          const BatchArg& bt = BatchArg());
 
+// slot of op j's output in a forward sweep that keeps every k-th state
+// (k = store_every): 0 -> ping-pong slots 0/1; 1 -> slot j; k > 1 -> the
+// checkpoint slot (j+1)/k - 1 when (j+1) % k == 0 or j is the last op,
+// otherwise one of two scratch slots after the n_ckpt checkpoints.
+__host__ __device__ __forceinline__ int64_t out_slot(int j, int n_ops, int k) {
+  if (k <= 0) return j & 1;
+  if (k == 1) return j;
+  const int64_t nc = (n_ops + k - 1) / k;
+  if ((j + 1) % k == 0) return (j + 1) / k - 1;
+  if (j == n_ops - 1) return nc - 1;
+  return nc + (j & 1);
+}
+
+// Persistent sweeps (sweep.cu): one cooperative launch walks every op of a
+// plan, all CTAs meeting at a grid barrier between ops.  For states small
+// enough that per-launch ramp and tail cost more than the op itself.
+struct SweepOp {
+  AxisView view;
+  int layout, mflags;
+  int64_t m_off;      // matrix in the arena (double2 entries)
+  int64_t c_off;      // the op's C entries in the C arena
+  int64_t part_base;  // the op's partial sums (double2 entries)
+  int nent;           // C entries
+  int fwd_nx;         // column tiles per block in the forward sweep
+  AdjSched sc;        // adjoint CTA schedule; sc.total <= grid
+};
+// grid-barrier state in device memory: arrival count, generation, error
+// flag, and one item counter per op (all zero at launch)
+struct SweepSync {
+  unsigned* count;
+  unsigned* gen;
+  int* err;
+  unsigned* items;
+};
+// CTAs per launch that can be co-resident (0: no persistent kernel for D)
+int sweep_grid(int dtype, int D, int backward);
+// adjoint schedule for a persistent sweep: every block's CTAs fit in `grid`
+AdjSched make_adj_sched_grid(int dtype, const AxisView& v, int D, int layout, int grid);
+int launch_sweep_forward(int dtype, int D, const SweepOp* ops, int n_ops, int store_every, const void* state_in,
+                         void* states, int64_t slot_elems, const double2* arena, SweepSync sync, int grid,
+                         cudaStream_t st);
+int launch_sweep_backward(int dtype, int D, const SweepOp* ops, int n_ops, const void* state_in, const void* states,
+                          int64_t slot_elems, void* lam_a, void* lam_b, const double2* arena, double2* cpart,
+                          double2* carena, int64_t carena_entries, SweepSync sync, int grid, cudaStream_t st);
+
 // reduced density matrix pieces (capi.cu)
 int launch_rdm_mixed(int dtype, const void* state, int num_modes, int D, int mode, int64_t ntr, int chunks,
                      double2* part, cudaStream_t st);

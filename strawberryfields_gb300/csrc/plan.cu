@@ -41,6 +41,9 @@ struct PlanOp {
   int plane = 0;
   PlaneGeom pg_fwd, pg_adj;
   int grid_fwd = 0, grid_adj = 0;
+  // persistent-sweep adjoint schedule and partial-sum region
+  AdjSched psched;
+  int64_t ppart_off = 0;
 };
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -61,6 +64,11 @@ struct fock_plan {
   int64_t arena_entries = 0, carena_entries = 0, cpart_entries = 0;
   int64_t state_elems = 0;
   int64_t flops_fwd = 0;
+  // persistent sweeps (small states): grids, tables, sync words, partials
+  int persist = 0;
+  int g_fwd = 0, g_bwd = 0;
+  size_t o_sweep = 0, o_sync = 0, o_ppart = 0;
+  int64_t ppart_entries = 0;
   // optional per-op timing
   int timing = 0;
   std::vector<cudaEvent_t> ev_fwd, ev_bwd;
@@ -293,6 +301,20 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   const char* kern = getenv("FOCK_GB300_KERNELS");
   const bool use_plane = !(kern && strcmp(kern, "block") == 0);
   const bool force_plane = kern && strcmp(kern, "plane") == 0;
+  // persistent sweeps for single circuits whose state is at most
+  // FOCK_GB300_SWEEP_MAX_BYTES (default 0: off -- on the 6-mode cutoff-12
+  // CV-QNN the per-op launches with programmatic dependent launch measured
+  // 2.3 ms per forward against 3.6 ms for the persistent sweep, whose grid
+  // barrier alone costs about 3 us per op)
+  const char* sw = getenv("FOCK_GB300_SWEEP_MAX_BYTES");
+  const int64_t sweep_max = sw ? (int64_t)atoll(sw) : 0;
+  const int64_t sbytes = elems * (dtype == FOCK_C64 ? 8 : 16);
+  if (batch == 1 && sbytes <= sweep_max && dmax_bucket(D) > 0) {
+    P->g_fwd = sweep_grid(dtype, D, 0);
+    P->g_bwd = sweep_grid(dtype, D, 1);
+    P->persist = P->g_fwd > 0 && P->g_bwd > 0;
+  }
+  int64_t ppart = 0;
   int64_t arena = 0, carena = 0, cpart = 0;
   int n_terms = 0, n_contrib = 0;
   for (size_t k = 0; k < P->ops.size(); ++k) {
@@ -316,6 +338,11 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
     if (op.plane) {
       op.grid_fwd = plane_grid(dtype, op.pg_fwd, 0, batch);
       op.grid_adj = plane_grid(dtype, op.pg_adj, 1, batch);
+    }
+    if (P->persist) {
+      op.psched = make_adj_sched_grid(dtype, op.view, D, op.layout, P->g_bwd);
+      op.ppart_off = ppart;
+      ppart += op.psched.part_entries;
     }
     op.c_off = carena;
     carena += op.nent;
@@ -341,10 +368,16 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   P->o_contrib = o; o = align256(o + sizeof(GradContrib) * std::max(n_contrib, 1));
   P->o_pstart = o; o = align256(o + sizeof(int) * (n_params + 1));
   P->o_plist = o; o = align256(o + sizeof(int) * std::max(n_contrib, 1));
+  if (P->persist) { P->o_sweep = o; o = align256(o + sizeof(SweepOp) * std::max(n_ops, 1)); }
   P->tables_bytes = o;
   P->o_arena = o; o = align256(o + sizeof(double2) * arena * batch);
   P->o_carena = o; o = align256(o + sizeof(double2) * std::max<int64_t>(carena, 1) * batch);
   P->o_cpart = o; o = align256(o + sizeof(double2) * std::max<int64_t>(cpart, 1) * batch);
+  if (P->persist) {
+    P->ppart_entries = ppart;
+    P->o_sync = o; o = align256(o + (4 + n_ops) * sizeof(unsigned));
+    P->o_ppart = o; o = align256(o + sizeof(double2) * std::max<int64_t>(ppart, 1));
+  }
   P->ws_bytes = o;
 
   if (cudaHostAlloc((void**)&P->host, P->tables_bytes, cudaHostAllocDefault) != cudaSuccess) {
@@ -388,6 +421,22 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
       contrib[c] = gc;
       by_param[gc.pidx].push_back(c);
       ++c;
+    }
+  }
+  if (P->persist) {
+    SweepOp* sw_ops = (SweepOp*)(P->host + P->o_sweep);
+    for (int k = 0; k < n_ops; ++k) {
+      const PlanOp& op = P->ops[k];
+      SweepOp& s = sw_ops[k];
+      s.view = op.view;
+      s.layout = op.layout;
+      s.mflags = op.swap ? MF_SWAP : 0;
+      s.m_off = op.m_off;
+      s.c_off = op.c_off;
+      s.part_base = op.ppart_off;
+      s.nent = (int)op.nent;
+      s.fwd_nx = (int)((op.view.ncols + 255) / 256);
+      s.sc = op.psched;
     }
   }
   int q = 0;
@@ -452,17 +501,15 @@ static int upload_and_build(fock_plan* P, const double* params, unsigned char* w
                            params, (double2*)(ws + P->o_arena), st, P->batch, P->n_params, P->arena_entries);
 }
 
-// slot of op j's output in a forward sweep that keeps every k-th state
-// (k = store_every): 0 -> ping-pong slots 0/1; 1 -> slot j; k > 1 -> the
-// checkpoint slot (j+1)/k - 1 when (j+1) % k == 0 or j is the last op,
-// otherwise one of two scratch slots after the n_ckpt checkpoints.
-static int64_t out_slot(int j, int n_ops, int k) {
-  if (k <= 0) return j & 1;
-  if (k == 1) return j;
-  const int64_t nc = (n_ops + k - 1) / k;
-  if ((j + 1) % k == 0) return (j + 1) / k - 1;
-  if (j == n_ops - 1) return nc - 1;
-  return nc + (j & 1);
+// grid-barrier words of a persistent sweep, cleared before every launch
+static int sweep_sync(fock_plan* P, unsigned char* ws, cudaStream_t st, SweepSync* s) {
+  unsigned* w = (unsigned*)(ws + P->o_sync);
+  FOCK_CUDA_TRY(cudaMemsetAsync(w, 0, (4 + P->ops.size()) * sizeof(unsigned), st));
+  s->count = w;
+  s->gen = w + 1;
+  s->err = (int*)(w + 2);
+  s->items = w + 4;
+  return FOCK_OK;
 }
 
 struct SweepCtx {
@@ -509,6 +556,13 @@ extern "C" int fock_plan_forward(fock_plan* P, const double* params, const void*
   sweep_ctx(P, ws, st, &c);
   const void* cur = state_in;
   const int n_ops = (int)P->ops.size();
+  if (P->persist && !P->timing && store_every <= 1 && n_ops > 0) {
+    SweepSync sync;
+    if ((rc = sweep_sync(P, ws, st, &sync))) return rc;
+    const int esz = P->dtype == FOCK_C64 ? 8 : 16;
+    return launch_sweep_forward(P->dtype, P->D, (const SweepOp*)(ws + P->o_sweep), n_ops, store_every, state_in,
+                                states, c.sb / esz, c.arena, sync, P->g_fwd, st);
+  }
   if (P->timing) {
     if ((rc = ensure_events(P->ev_fwd, n_ops + 1))) return rc;
     P->fwd_recorded = 0;
@@ -527,6 +581,15 @@ extern "C" int fock_plan_forward(fock_plan* P, const double* params, const void*
     if ((rc = record_event(P->ev_fwd[n_ops], st))) return rc;
     P->fwd_recorded = 1;
   }
+  return FOCK_OK;
+}
+
+static int param_grads(fock_plan* P, unsigned char* ws, const SweepCtx& c, double* grad_params, cudaStream_t st) {
+  if (P->n_params > 0)
+    return launch_param_grads((const GradOp*)(ws + P->o_gops), (const GradContrib*)(ws + P->o_contrib),
+                              (const int*)(ws + P->o_pstart), (const int*)(ws + P->o_plist), P->n_params,
+                              (const PhaseTerm*)(ws + P->o_terms), c.arena, (const double2*)(ws + P->o_carena),
+                              grad_params, st, P->batch, P->arena_entries, P->carena_entries);
   return FOCK_OK;
 }
 
@@ -550,6 +613,19 @@ extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void
   const int K = store_every;
   void* lam = grad_state;
   void* other = grad_tmp;
+  if (P->persist && !P->timing && K == 1 && n_ops > 0) {
+    SweepSync sync;
+    if ((rc = sweep_sync(P, ws, st, &sync))) return rc;
+    const int esz = P->dtype == FOCK_C64 ? 8 : 16;
+    rc = launch_sweep_backward(P->dtype, P->D, (const SweepOp*)(ws + P->o_sweep), n_ops, state_in, states,
+                               c.sb / esz, grad_state, grad_tmp, c.arena, (double2*)(ws + P->o_ppart),
+                               (double2*)(ws + P->o_carena), P->carena_entries, sync, P->g_bwd, st);
+    if (rc) return rc;
+    // op n-1 reads grad_state, writes grad_tmp; the final lam_in is in
+    // grad_state when n_ops is even
+    if (n_ops & 1) FOCK_CUDA_TRY(cudaMemcpyAsync(grad_state, grad_tmp, c.sb, cudaMemcpyDeviceToDevice, st));
+    return param_grads(P, ws, c, grad_params, st);
+  }
   if (P->timing) {
     if ((rc = ensure_events(P->ev_bwd, n_ops + 1))) return rc;
     P->bwd_recorded = 0;
@@ -606,12 +682,23 @@ extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void
     P->bwd_recorded = 1;
   }
   if (lam != grad_state) FOCK_CUDA_TRY(cudaMemcpyAsync(grad_state, lam, c.sb, cudaMemcpyDeviceToDevice, st));
-  if (P->n_params > 0) {
-    rc = launch_param_grads((const GradOp*)(ws + P->o_gops), (const GradContrib*)(ws + P->o_contrib),
-                            (const int*)(ws + P->o_pstart), (const int*)(ws + P->o_plist), P->n_params,
-                            (const PhaseTerm*)(ws + P->o_terms), c.arena, (const double2*)(ws + P->o_carena),
-                            grad_params, st, P->batch, P->arena_entries, P->carena_entries);
-    if (rc) return rc;
+  return param_grads(P, ws, c, grad_params, st);
+  return FOCK_OK;
+}
+
+extern "C" int fock_plan_sweep_status(const fock_plan* P, const void* workspace, int* grids, int* error) {
+  if (!P) return fock_set_error(FOCK_ERR_INVALID, "null plan");
+  if (grids) {
+    grids[0] = P->persist ? P->g_fwd : 0;
+    grids[1] = P->persist ? P->g_bwd : 0;
+  }
+  if (error) {
+    *error = 0;
+    if (P->persist) {
+      if (!workspace) return fock_set_error(FOCK_ERR_INVALID, "null workspace");
+      FOCK_CUDA_TRY(cudaMemcpy(error, (const unsigned char*)workspace + P->o_sync + 2 * sizeof(unsigned),
+                               sizeof(int), cudaMemcpyDeviceToHost));
+    }
   }
   return FOCK_OK;
 }
