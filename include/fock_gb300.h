@@ -155,7 +155,13 @@ int fock_reduced_dm1_noalloc(int num_modes, int cutoff, int pure, int dtype, int
 /* ---------------------------------------------- compiled circuits + adjoint (A1-A3)
  * A plan is a gate list compiled on the host: rotation/Kerr/cross-Kerr gates
  * are fused into the neighbouring non-diagonal gate, so the state crosses HBM
- * once per remaining op.
+ * once per remaining op.  pure = 0 compiles for density matrices [D]^(2n)
+ * with interleaved (ket, bra) axes: every unitary op is applied as M on its
+ * ket axes and conj(M) on its bra axes (one matrix build, two ops), and
+ * FOCK_LOSS gates (parameter T) become the loss superoperator on the mode's
+ * (ket, bra) pair -- fockbackend/circuit.py:186-217 and :65-87; phases next
+ * to a loss are carried by it (+p on the ket, -p on the bra).  A plan's ops
+ * (fock_plan_op) are these applications.
  * Forward: op k maps the previous state to its output; `store_every` = k
  * decides which outputs are kept in `states` (slots of batch * D^n entries):
  * 0 -> two ping-pong slots (final state in slot (n_ops-1) & 1); 1 -> every

@@ -456,6 +456,7 @@ def reduced_dm(state, n, mode, pure=True):
 # ---------------------------------------------------------------------------
 # gate kinds (same codes as the C ABI)
 ROTATION, KERR, DISPLACEMENT, SQUEEZE, BEAMSPLITTER, TWO_MODE_SQUEEZE, MZGATE, CROSS_KERR = 1, 2, 3, 4, 5, 6, 7, 8
+LOSS = 9
 
 
 def gate_matrix(kind, p, D):
@@ -498,7 +499,7 @@ def gate_matrix(kind, p, D):
 
 
 NPARAMS = {ROTATION: 1, KERR: 1, DISPLACEMENT: 2, SQUEEZE: 2, BEAMSPLITTER: 2, TWO_MODE_SQUEEZE: 2,
-           MZGATE: 2, CROSS_KERR: 1}
+           MZGATE: 2, CROSS_KERR: 1, LOSS: 1}
 
 
 def run_gates(gates, params, N, D, state=None):
@@ -515,6 +516,21 @@ def run_gates(gates, params, N, D, state=None):
             psi = apply_gate2(psi, U, m1, m2)
         out.append(psi)
     return out
+
+
+def run_gates_mixed(gates, params, N, D, rho=None):
+    """Density-matrix run of a gate list (vacuum by default): unitaries as
+    ``U rho U^dag`` (reference circuit.py:186-217), ``LOSS`` (parameter T) as
+    the Kraus sum of circuit.py:65-87.  Returns the final rho."""
+    rho = vacuum(N, D, pure=False) if rho is None else np.array(rho, dtype=CDT)
+    for kind, m1, m2, pi in gates:
+        p = [params[pi + k] for k in range(NPARAMS[kind])]
+        if kind == LOSS:
+            rho = apply_loss(rho, p[0], m1, N, pure=False)
+            continue
+        U, _ = gate_matrix(kind, p, D)
+        rho = apply_gate1(rho, U, m1, pure=False) if U.ndim == 2 else apply_gate2(rho, U, m1, m2, pure=False)
+    return rho
 
 
 def adjoint_grads(gates, params, N, D, grad_final, state=None):

@@ -44,10 +44,13 @@ class CompiledCircuit:
             adjoint sweep and recompute the others segment by segment (1 keeps
             all outputs; larger values trade one extra forward for
             ``n_ops / checkpoint + checkpoint`` resident states instead of ``n_ops``)
+        pure (bool): ket ``[D]*n`` (default) or density matrix ``[D]*(2n)``
+            with interleaved (ket, bra) axes; mixed circuits may contain
+            ``LOSS`` gates (parameter T)
     """
 
     def __init__(self, num_modes, cutoff, gates, n_params, dtype=torch.complex64, device=None, batch=1,
-                 checkpoint=1):
+                 checkpoint=1, pure=True):
         lib = L.load()
         self.num_modes = int(num_modes)
         self.cutoff = int(cutoff)
@@ -61,16 +64,18 @@ class CompiledCircuit:
         plan = ctypes.c_void_p()
         self.batch = int(batch)
         self.checkpoint = int(checkpoint)
+        self.pure = bool(pure)
         if self.checkpoint < 1:
             raise ValueError("checkpoint must be >= 1")
-        L.check(lib.fock_plan_create_batch(self.num_modes, self.cutoff, 1, self._dcode, arr, len(gates),
-                                           self.n_params, self.batch, ctypes.byref(plan)), "fock_plan_create")
+        L.check(lib.fock_plan_create_batch(self.num_modes, self.cutoff, 1 if self.pure else 0, self._dcode, arr,
+                                           len(gates), self.n_params, self.batch, ctypes.byref(plan)),
+                "fock_plan_create")
         self._plan = plan
         info = L.PlanInfo()
         L.check(lib.fock_plan_get_info(plan, ctypes.byref(info)), "fock_plan_get_info")
         self.info = info
         self.n_gates = len(gates)
-        self.shape = [self.cutoff] * self.num_modes
+        self.shape = [self.cutoff] * (self.num_modes if self.pure else 2 * self.num_modes)
         self._bshape = ([self.batch] if self.batch > 1 else []) + self.shape
         self._ws_buf = None
         self._vacuum = torch.zeros([self.batch, int(info.state_elems)], dtype=self.dtype, device=self.device)

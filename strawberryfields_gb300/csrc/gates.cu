@@ -405,21 +405,29 @@ __device__ void build_mzgate(double phi_in, int D, double2* M, double2* dM, doub
 // N(T){|n><m|} = sum_l c(n,m,l) |n-l><m-l|,
 // c = (1-T)^l T^{(n+m)/2 - l} / l! sqrt(n! m! / ((n-l)! (m-l)!))
 // (strawberryfields/ops.py:1369-1376; Kraus form fockbackend/ops.py:471).
-__device__ void build_loss(double T, int D, double2* M) {
+// dM = dc/dT = (-l (1-T)^(l-1) T^ex + ex (1-T)^l T^(ex-1)) * (the factorials)
+// with ex = (n+m)/2 - l.
+__device__ void build_loss(double T, int D, double2* M, double2* dM) {
   const int tot = blk_total(D);
   for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
     int oa, ob, ia, ib, u, v, b;
     entry_coords(LAYOUT_DIFF, D, idx, oa, ob, ia, ib, u, v, b);
-    double val = 0.0;
+    double val = 0.0, dval = 0.0;
     int l = ia - oa;
     if (l >= 0 && ib - ob == l) {
       int n = ia, m = ib;
       double lg = 0.5 * (lgamma(n + 1.0) + lgamma(m + 1.0) - lgamma(n - l + 1.0) - lgamma(m - l + 1.0)) -
                   lgamma(l + 1.0);
       double ex = 0.5 * (n + m) - l;
-      val = pow(1.0 - T, (double)l) * pow(T, ex) * exp(lg);
+      const double f = exp(lg);
+      val = pow(1.0 - T, (double)l) * pow(T, ex) * f;
+      double d = 0.0;
+      if (l > 0) d -= l * pow(1.0 - T, (double)(l - 1)) * pow(T, ex);
+      if (ex > 0.0) d += ex * pow(1.0 - T, (double)l) * pow(T, ex - 1.0);
+      dval = d * f;
     }
     M[idx] = make_double2(val, 0.0);
+    if (dM) dM[idx] = make_double2(dval, 0.0);
   }
   __syncthreads();
 }
@@ -472,7 +480,7 @@ __device__ void run_build_job(const BuildJob& J, const PhaseTerm* terms, const d
       blocks_truncate_and_derive(X, D, 0, p1, 1, M, dM);
       break;
     case FOCK_MZGATE: build_mzgate(p0, D, M, dM, X); break;
-    case FOCK_LOSS: build_loss(p0, D, M); break;
+    case FOCK_LOSS: build_loss(p0, D, M, dM); break;
     case FOCK_ROTATION:
     case FOCK_KERR:
     case FOCK_CROSS_KERR: build_diag_gate(J.gate, p0, J.layout, D, M); break;
@@ -488,6 +496,7 @@ __device__ void run_build_job(const BuildJob& J, const PhaseTerm* terms, const d
       for (int k = 0; k < J.nterm; ++k) {
         const PhaseTerm& P = terms[J.term0 + k];
         double pv = P.pidx >= 0 ? params[P.pidx] : P.value;
+        if (P.neg) pv = -pv;
         ang += pv * (P.side ? phase_fn(P.fn, oa, ob) : phase_fn(P.fn, ia, ib));
       }
       double2 ph = dexpi(ang);
@@ -586,6 +595,7 @@ __global__ void param_grads_kernel(const GradOp* ops, const GradContrib* contrib
         x = make_double2(-m.y * w, m.x * w);  // i w M
       }
       double2 c = C[e];
+      if (O.conj) c.y = -c.y;        // Re(C conj(dM)) = Re(conj(C) dM) for a conj(M) op
       acc += c.x * x.x - c.y * x.y;  // Re(c x)
     }
     red[threadIdx.x] = acc;

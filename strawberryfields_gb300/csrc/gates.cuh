@@ -26,12 +26,13 @@ __host__ __device__ __forceinline__ double phase_fn(int fn, int a, int b) {
 }
 
 // exp(i * value * f(coords)) applied to the input (side 0) or output (side 1)
-// coordinates of every entry.  value = params[pidx] when pidx >= 0.
+// coordinates of every entry.  value = params[pidx] when pidx >= 0; neg
+// negates it (the bra half of a phase on a density-matrix superoperator).
 struct PhaseTerm {
   int fn;
   int side;
   int pidx;
-  int pad_;
+  int neg;
   double value;
 };
 
@@ -69,6 +70,7 @@ struct GradOp {
   int64_t m_off, dm_off;  // arena offsets
   int64_t c_off;          // offset of the reduced C matrix (double2) in the C arena
   int nent;
+  int conj;               // the op applied conj(M) (bra side of a density matrix): use conj(C)
 };
 
 int64_t layout_entries(int layout, int D);

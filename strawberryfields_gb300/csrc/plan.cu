@@ -29,6 +29,11 @@ struct PlanOp {
   int mode1 = -1, mode2 = -1;
   int pidx = -1;
   int n_fused = 0;
+  // state axes the op acts on (modes for a ket; 2m / 2m+1 for the ket / bra
+  // side of a density matrix), bra-side flag, and the op whose matrix it uses
+  int axis_a = -1, axis_b = -1;
+  int conj = 0;
+  int owner = -1;
   std::vector<PhaseTerm> terms;
   std::vector<GradContrib> contribs;  // .op filled at finalize
   // derived
@@ -48,10 +53,14 @@ struct PlanOp {
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// matrix staging flags of an op: swapped view axes, bra side (conj M)
+inline int op_flags(const PlanOp& op) { return (op.swap ? MF_SWAP : 0) | (op.conj ? MF_CONJ : 0); }
+
 }  // namespace
 
 struct fock_plan {
   int N = 0, D = 0, pure = 1, dtype = 0, n_params = 0, n_gates = 0;
+  int n_jobs = 0;  // matrix builds (ops that own a matrix)
   int batch = 1;  // circuits of this structure run together (grid.z)
   std::vector<PlanOp> ops;
   // table image (pinned host memory) and its sections
@@ -103,16 +112,25 @@ static int is_two(int k) {
 }
 
 // add a phase term (with its gradient contribution) to op
-static void add_term(PlanOp& op, int fn, int side, int pidx) {
-  op.terms.push_back(PhaseTerm{fn, side, pidx, 0, 0.0});
+static void add_term(PlanOp& op, int fn, int side, int pidx, int neg = 0) {
+  op.terms.push_back(PhaseTerm{fn, side, pidx, neg, 0.0});
   GradContrib g;
   g.op = -1;
   g.type = side ? GC_W_OUT : GC_W_IN;
   g.fn = fn;
   g.pidx = pidx;
-  g.scale = 1.0;
+  g.scale = neg ? -1.0 : 1.0;
   op.contribs.push_back(g);
   op.n_fused++;
+}
+
+// a phase on mode m of a density matrix, carried by the loss superoperator
+// on the (ket, bra) pair: exp(i p f(n_ket)) on the ket axis and
+// exp(-i p f(n_bra)) on the bra axis
+static void add_loss_terms(PlanOp& op, int fn, int side, int pidx) {
+  add_term(op, fn, side, pidx, 0);
+  add_term(op, fn == FN_A ? FN_B : FN_B2, side, pidx, 1);
+  op.n_fused--;
 }
 
 static void add_contrib(PlanOp& op, int type, int fn, int pidx, double scale) {
@@ -135,6 +153,11 @@ struct PendingCK {
 
 // move pending single-mode terms of `mode` into op as input-side terms
 static void absorb_pending(PlanOp& op, int mode, std::vector<std::vector<Pending>>& pend) {
+  if (op.gate == FOCK_LOSS) {
+    for (const Pending& p : pend[mode]) add_loss_terms(op, p.fn, 0, p.pidx);
+    pend[mode].clear();
+    return;
+  }
   const int slot_b = (op.layout != LAYOUT_DENSE && op.mode2 == mode);
   for (const Pending& p : pend[mode]) {
     int fn = p.fn;
@@ -157,10 +180,10 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   if (dtype != FOCK_C64 && dtype != FOCK_C128) return fock_set_error(FOCK_ERR_INVALID, "bad dtype");
   if (cutoff < 1 || cutoff > FOCK_MAX_CUTOFF) return fock_set_error(FOCK_ERR_INVALID, "bad cutoff %d", cutoff);
   if (num_modes < 1 || num_modes > FOCK_MAX_AXES / 2) return fock_set_error(FOCK_ERR_INVALID, "bad number of modes");
-  if (!pure) return fock_set_error(FOCK_ERR_UNSUPPORTED, "compiled circuits support pure states");
   if (n_gates < 0 || (n_gates > 0 && !gates)) return fock_set_error(FOCK_ERR_INVALID, "bad gate list");
   if (n_params < 0) return fock_set_error(FOCK_ERR_INVALID, "bad parameter count");
-  if (num_modes * log2((double)cutoff) > 60.0) return fock_set_error(FOCK_ERR_INVALID, "state too large");
+  const int naxes = pure ? num_modes : 2 * num_modes;
+  if (naxes * log2((double)cutoff) > 60.0) return fock_set_error(FOCK_ERR_INVALID, "state too large");
 
   fock_plan* P = new fock_plan();
   P->batch = batch;
@@ -199,7 +222,7 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
     if (two && (G.mode2 < 0 || G.mode2 >= N || G.mode2 == G.mode1)) return fail(FOCK_ERR_INVALID, "invalid second mode", g);
     const int np = (G.kind == FOCK_ROTATION || G.kind == FOCK_KERR || G.kind == FOCK_CROSS_KERR || G.kind == FOCK_LOSS) ? 1 : 2;
     if (G.pidx < 0 || G.pidx + np > n_params) return fail(FOCK_ERR_INVALID, "parameter index out of range", g);
-    if (G.kind == FOCK_LOSS) return fail(FOCK_ERR_UNSUPPORTED, "loss channel in a pure-state circuit", g);
+    if (G.kind == FOCK_LOSS && pure) return fail(FOCK_ERR_UNSUPPORTED, "loss channel in a pure-state circuit", g);
     if (is_diag1(G.kind)) {
       pend[G.mode1].push_back(Pending{G.kind == FOCK_ROTATION ? FN_A : FN_A2, G.pidx});
       continue;
@@ -259,6 +282,10 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
         add_term(op, FN_A, 0, G.pidx + 1);
         op.n_fused--;  // part of the gate itself
         break;
+      case FOCK_LOSS:
+        // superoperator on the mode's (ket, bra) pair; dM = d/dT
+        add_contrib(op, GC_DM, 0, G.pidx, 1.0);
+        break;
       default:
         break;
     }
@@ -285,6 +312,10 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
     PlanOp& op = P->ops[last_op[m]];
     const int slot_b = (op.layout != LAYOUT_DENSE && op.mode2 == m);
     for (const Pending& p : pend[m]) {
+      if (op.gate == FOCK_LOSS) {
+        add_loss_terms(op, p.fn, 1, p.pidx);
+        continue;
+      }
       int fn = p.fn;
       if (slot_b) fn = (fn == FN_A) ? FN_B : FN_B2;
       add_term(op, fn, 1, p.pidx);
@@ -292,9 +323,43 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
     pend[m].clear();
   }
 
+  // state axes of every op; a density matrix applies each unitary op on the
+  // ket axes with M and on the bra axes with conj(M) (one matrix, two
+  // launches), the loss superoperator once on the mode's (ket, bra) pair
+  if (pure) {
+    for (PlanOp& op : P->ops) {
+      op.axis_a = op.mode1;
+      op.axis_b = op.mode2;
+    }
+  } else {
+    std::vector<PlanOp> ex;
+    for (const PlanOp& op : P->ops) {
+      if (op.gate == FOCK_LOSS) {
+        PlanOp l = op;
+        l.axis_a = 2 * op.mode1;
+        l.axis_b = 2 * op.mode1 + 1;
+        ex.push_back(l);
+        continue;
+      }
+      PlanOp ket = op;
+      ket.axis_a = 2 * op.mode1;
+      ket.axis_b = op.mode2 >= 0 ? 2 * op.mode2 : -1;
+      ex.push_back(ket);
+      PlanOp bra = op;
+      bra.axis_a = 2 * op.mode1 + 1;
+      bra.axis_b = op.mode2 >= 0 ? 2 * op.mode2 + 1 : -1;
+      bra.conj = 1;
+      bra.owner = (int)ex.size() - 1;
+      bra.n_fused = 0;
+      bra.terms.clear();  // built once, by the ket op
+      ex.push_back(bra);
+    }
+    P->ops = ex;
+  }
+
   // layout of arena / C arena / partials, and tables
   int64_t elems = 1;
-  for (int k = 0; k < N; ++k) elems *= D;
+  for (int k = 0; k < naxes; ++k) elems *= D;
   P->state_elems = elems;
   // kernel family per op: plane-tile kernels where plane_preferred says so;
   // FOCK_GB300_KERNELS=block / plane forces one family (where it applies)
@@ -320,17 +385,24 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   for (size_t k = 0; k < P->ops.size(); ++k) {
     PlanOp& op = P->ops[k];
     op.nent = layout_entries(op.layout, D);
-    op.m_off = arena;
-    arena += op.nent;
-    const bool has_dm = op.gate != GATE_IDENTITY;
-    if (has_dm) { op.dm_off = arena; arena += op.nent; }
-    const int64_t ns = build_scratch_entries(op.gate, D);
-    if (ns > 0) { op.scratch_off = arena; arena += ns; }
-    if (op.layout == LAYOUT_DENSE) op.view = make_view1(N, D, op.mode1);
+    if (op.owner >= 0) {
+      const PlanOp& ow = P->ops[op.owner];
+      op.m_off = ow.m_off;
+      op.dm_off = ow.dm_off;
+      op.scratch_off = ow.scratch_off;
+    } else {
+      op.m_off = arena;
+      arena += op.nent;
+      const bool has_dm = op.gate != GATE_IDENTITY;
+      if (has_dm) { op.dm_off = arena; arena += op.nent; }
+      const int64_t ns = build_scratch_entries(op.gate, D);
+      if (ns > 0) { op.scratch_off = arena; arena += ns; }
+    }
+    if (op.layout == LAYOUT_DENSE) op.view = make_view1(naxes, D, op.axis_a);
     else {
-      int a = op.mode1, b = op.mode2;
+      int a = op.axis_a, b = op.axis_b;
       op.swap = a > b;
-      op.view = make_view2(N, D, std::min(a, b), std::max(a, b));
+      op.view = make_view2(naxes, D, std::min(a, b), std::max(a, b));
     }
     op.sched = make_adj_sched(dtype, op.view, D, op.layout);
     op.plane = use_plane && (force_plane || plane_preferred(op.layout, op.view)) && make_plane_geom(dtype, op.view, D, op.layout, op.swap, 0, &op.pg_fwd) &&
@@ -362,7 +434,9 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   P->n_contrib = n_contrib;
   const int n_ops = (int)P->ops.size();
   size_t o = 0;
-  P->o_jobs = o; o = align256(o + sizeof(BuildJob) * std::max(n_ops, 1));
+  P->n_jobs = 0;
+  for (const PlanOp& op : P->ops) P->n_jobs += op.owner < 0;
+  P->o_jobs = o; o = align256(o + sizeof(BuildJob) * std::max(P->n_jobs, 1));
   P->o_terms = o; o = align256(o + sizeof(PhaseTerm) * std::max(n_terms, 1));
   P->o_gops = o; o = align256(o + sizeof(GradOp) * std::max(n_ops, 1));
   P->o_contrib = o; o = align256(o + sizeof(GradContrib) * std::max(n_contrib, 1));
@@ -393,22 +467,24 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   GradContrib* contrib = (GradContrib*)(P->host + P->o_contrib);
   int* pstart = (int*)(P->host + P->o_pstart);
   int* plist = (int*)(P->host + P->o_plist);
-  int t = 0, c = 0;
+  int t = 0, c = 0, nj = 0;
   std::vector<std::vector<int>> by_param(n_params);
   for (int k = 0; k < n_ops; ++k) {
     PlanOp& op = P->ops[k];
-    BuildJob& J = jobs[k];
-    J.gate = op.gate;
-    J.layout = op.layout;
-    J.D = D;
-    J.pidx = op.pidx;
-    J.v0 = J.v1 = 0.0;
-    J.term0 = t;
-    J.nterm = (int)op.terms.size();
-    J.m_off = op.m_off;
-    J.dm_off = op.dm_off;
-    J.scratch_off = op.scratch_off;
-    for (const PhaseTerm& pt : op.terms) terms[t++] = pt;
+    if (op.owner < 0) {  // builds its matrix (bra-side ops reuse the ket op's)
+      BuildJob& J = jobs[nj++];
+      J.gate = op.gate;
+      J.layout = op.layout;
+      J.D = D;
+      J.pidx = op.pidx;
+      J.v0 = J.v1 = 0.0;
+      J.term0 = t;
+      J.nterm = (int)op.terms.size();
+      J.m_off = op.m_off;
+      J.dm_off = op.dm_off;
+      J.scratch_off = op.scratch_off;
+      for (const PhaseTerm& pt : op.terms) terms[t++] = pt;
+    }
     GradOp& go = gops[k];
     go.layout = op.layout;
     go.D = D;
@@ -416,6 +492,7 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
     go.dm_off = op.dm_off;
     go.c_off = op.c_off;
     go.nent = (int)op.nent;
+    go.conj = op.conj;
     for (GradContrib gc : op.contribs) {
       gc.op = k;
       contrib[c] = gc;
@@ -430,7 +507,7 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
       SweepOp& s = sw_ops[k];
       s.view = op.view;
       s.layout = op.layout;
-      s.mflags = op.swap ? MF_SWAP : 0;
+      s.mflags = op_flags(op);
       s.m_off = op.m_off;
       s.c_off = op.c_off;
       s.part_base = op.ppart_off;
@@ -497,7 +574,7 @@ static int upload_and_build(fock_plan* P, const double* params, unsigned char* w
     // table; building dM as well costs one extra matrix write per op and keeps
     // one table
   }
-  return launch_build_jobs((const BuildJob*)(ws + P->o_jobs), n_ops, (const PhaseTerm*)(ws + P->o_terms),
+  return launch_build_jobs((const BuildJob*)(ws + P->o_jobs), P->n_jobs, (const PhaseTerm*)(ws + P->o_terms),
                            params, (double2*)(ws + P->o_arena), st, P->batch, P->n_params, P->arena_entries);
 }
 
@@ -536,9 +613,9 @@ static int sweep_ctx(fock_plan* P, unsigned char* ws, cudaStream_t st, SweepCtx*
 static int apply_op(const SweepCtx& c, int k, const void* in, void* out) {
   const PlanOp& op = c.P->ops[k];
   if (op.plane)
-    return launch_plane_apply(c.P->dtype, in, out, op.pg_fwd, op.grid_fwd, c.arena + op.m_off, op.swap ? MF_SWAP : 0,
+    return launch_plane_apply(c.P->dtype, in, out, op.pg_fwd, op.grid_fwd, c.arena + op.m_off, op_flags(op),
                               c.st, c.bt);
-  return launch_apply(c.P->dtype, in, out, op.view, c.P->D, op.layout, c.arena + op.m_off, op.swap ? MF_SWAP : 0,
+  return launch_apply(c.P->dtype, in, out, op.view, c.P->D, op.layout, c.arena + op.m_off, op_flags(op),
                       c.st, c.bt);
 }
 
@@ -659,13 +736,13 @@ extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void
       double2* cout = (double2*)(ws + P->o_carena) + op.c_off;
       if (op.plane) {
         rc = launch_plane_adjoint(P->dtype, psi_in, lam, other, op.pg_adj, op.grid_adj, c.arena + op.m_off,
-                                  op.swap ? MF_SWAP : 0, cpart, st, c.bt);
+                                  op_flags(op), cpart, st, c.bt);
         if (rc) return rc;
         rc = launch_reduce_partials(cpart, op.grid_adj, op.nent, cout, st, P->batch, P->cpart_entries,
                                     P->carena_entries, pdl);
       } else {
         rc = launch_adjoint_partials(P->dtype, psi_in, lam, other, op.view, P->D, op.layout, c.arena + op.m_off,
-                                     op.swap ? MF_SWAP : 0, cpart, op.sched, st, c.bt);
+                                     op_flags(op), cpart, op.sched, st, c.bt);
         if (rc) return rc;
         rc = launch_reduce_sched(cpart, op.sched, P->D, op.layout, cout, st, P->batch, P->cpart_entries,
                                  P->carena_entries, pdl);

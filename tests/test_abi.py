@@ -140,8 +140,27 @@ def test_plan_rejects_bad_gate_lists(lib):
     for gates, npar in [([(3, 4, -1, 0)], 2), ([(5, 0, 0, 0)], 2), ([(3, 0, -1, 1)], 2), ([(42, 0, -1, 0)], 2)]:
         rc, plan = _plan(gates, npar)
         assert rc == _lib.FOCK_ERR_INVALID
-    rc, plan = _plan([(3, 0, -1, 0)], 2, pure=0)
+    # a loss channel needs a density matrix
+    rc, plan = _plan([(9, 0, -1, 0)], 1)
     assert rc == _lib.FOCK_ERR_UNSUPPORTED
+
+
+def test_mixed_plan_structure(lib):
+    """Density-matrix plans: each unitary op runs on the ket axes and, with the
+    conjugate matrix, on the bra axes; a loss channel is one superoperator op;
+    phases next to a loss are carried by it."""
+    # S(0), BS(0,1), K(1), loss(1), R(0)
+    gates = [(4, 0, -1, 0), (5, 0, 1, 2), (2, 1, -1, 4), (9, 1, -1, 5), (1, 0, -1, 6)]
+    rc, plan = _plan(gates, 7, pure=0)
+    assert rc == 0
+    info, ops = _ops(plan)
+    kinds = [(o[0], o[1], o[2]) for o in ops]
+    assert kinds == [(1, 0, -1), (1, 0, -1), (2, 0, 1), (2, 0, 1), (3, 1, -1)]
+    # every gate accounted for once (bra-side ops carry no fused count); the
+    # trailing rotation on mode 0 rides on the beamsplitter's ket op
+    assert sum(o[3] for o in ops) == len(gates)
+    assert info.state_elems == 6 ** 6 and info.n_ops == 5  # 3 modes, D = 6, density matrix
+    lib.fock_plan_destroy(plan)
 
 
 def test_product_path_has_no_cpu_fallback():

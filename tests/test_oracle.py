@@ -175,3 +175,27 @@ def test_oracle_vs_reference_circuit():
     N, D, pure, ops = mg.pure_all(1)
     ref, _ = mg.run_reference(N, D, pure, ops)
     assert np.abs(oracle_run(N, D, pure, ops) - ref).max() < 1e-13
+
+
+def test_oracle_mixed_gate_list_matches_golden():
+    """The oracle's density-matrix gate-list runner reproduces the mixed golden
+    vectors (unitaries on ket and bra axes, loss channels) of the reference
+    Circuit."""
+    import os
+
+    from tests.gatelist import ops_to_gates
+    from tests.golden.make_golden import decode
+
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    n = 0
+    for f in sorted(os.listdir(golden)):
+        if not f.endswith(".npz"):
+            continue
+        z = np.load(os.path.join(golden, f))
+        if bool(z["pure"]):
+            continue
+        gates, params = ops_to_gates(decode(z["ops"]))
+        rho = fo.run_gates_mixed(gates, params, int(z["N"]), int(z["D"]))
+        assert np.abs(rho - z["state"]).max() < 1e-12, f
+        n += 1
+    assert n >= 2
