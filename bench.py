@@ -448,6 +448,95 @@ def single_gate_case(args):
     return 0
 
 
+def lossy_case(args):
+    """Mixed-state lossy gradient: 4-mode cutoff-14 density matrix (14^8
+    complex64 entries, 11.8 GB), 6 CV-QNN layers with a loss channel on every
+    mode per layer; loss = mean photon number of mode 0; forward checkpoints
+    every 2 layers, each 2-layer segment recomputed recursively in the device
+    memory left (a pool of `slots` states).  A step is one forward + one
+    adjoint gradient of all parameters.  Checked by the trace of rho and a
+    central-difference directional derivative (complex64 forward, h = 1e-2)."""
+    import torch
+
+    from strawberryfields_gb300 import CompiledCircuit
+    from strawberryfields_gb300.qnn import lossy_qnn_gates, qnn_params
+
+    dev = torch.device("cuda", 0)
+    N, D, layers = 4, 14, 6
+    gates, npar = lossy_qnn_gates(N, layers)
+    params = torch.tensor(qnn_params(gates, npar, seed=0), device=dev)
+    # ops per 2 layers (independent of the cutoff)
+    n_ops = CompiledCircuit(N, 2, gates, npar, dtype=torch.complex64, device=dev, pure=False).n_ops
+    k = 2 * n_ops // layers
+    S = 8 * D ** (2 * N)
+    free, _ = torch.cuda.mem_get_info(dev)
+    n_ckpt = -(-n_ops // k) + 2
+    # states: checkpoints + scratch, vacuum input, adjoint pair, pool
+    slots = int(min(k - 1, (free - (6 << 30)) // S - n_ckpt - 3))
+    if slots < 3:
+        print(json.dumps({"case": "lossy", "unavailable": f"{free / 1e9:.0f} GB free: fewer than 3 recompute slots"}))
+        return 0
+    circ = CompiledCircuit(N, D, gates, npar, dtype=torch.complex64, device=dev, pure=False, checkpoint=k,
+                           recompute_slots=slots)
+    nvec = torch.arange(D, device=dev, dtype=torch.float32)
+
+    def diag(rho):
+        d = rho
+        for _ in range(N):
+            d = torch.diagonal(d, dim1=0, dim2=1)
+        return d  # [D]*N, views only
+
+    def step():
+        states = circ.forward_states(params)
+        rho = states[circ.final_index()]
+        loss = torch.sum(nvec.reshape(D, 1, 1, 1) * diag(rho).real)
+        trace = torch.sum(diag(rho).real)
+        g = torch.zeros_like(rho)
+        diag(g).copy_(nvec.reshape(D, 1, 1, 1).expand(D, D, D, D).to(g.dtype))
+        del rho
+        grads, _ = circ.backward(params, states, g, overwrite_grad=True)
+        del states, g
+        return loss, trace, grads
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times = []
+    for _ in range(args.steps):
+        e0.record()
+        loss, trace, grads = step()
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = float(np.median(times))
+    # directional derivative against central differences of the forward
+    v = torch.tensor(np.random.default_rng(1).normal(size=npar), device=dev)
+    v /= torch.linalg.vector_norm(v)
+    h = 1e-2
+
+    def fwd_loss(pp):
+        st = circ.forward_states(pp, store_all=False)
+        return float(torch.sum(nvec.reshape(D, 1, 1, 1) * diag(st).real))
+
+    fd = (fwd_loss(params + h * v) - fwd_loss(params - h * v)) / (2 * h)
+    ad = float(torch.dot(grads, v))
+    fwd_ops = n_ops
+    print(json.dumps({
+        "case": "lossy", "metric": "mixed-state lossy gradients/s", "value": 1.0 / t, "unit": "grads/s",
+        "s_per_gradient": t, "steps": args.steps, "warmup": args.warmup,
+        "config": {"workload": "4-mode cutoff-14 lossy CV-QNN gradient", "modes": N, "cutoff": D,
+                   "layers": layers, "state": f"density matrix 14^8 complex64 ({S / 1e9:.1f} GB)",
+                   "gates": len(gates), "params": npar, "ops": n_ops, "checkpoint_every_ops": k,
+                   "recompute_slots": slots, "loss": "<n_0>"},
+        "loss": float(loss), "trace": float(trace),
+        "directional_derivative": {"adjoint": ad, "central_difference": fd,
+                                   "rel_err": abs(ad - fd) / max(abs(fd), 1e-30)},
+        "state_bytes": S, "forward_op_bytes": 2 * S * fwd_ops,
+    }))
+    return 0
+
+
 def batched_case(args):
     """4096 independent CV-QNN circuits, modes U{2..5}, cutoff U{6..20}, depth
     U{2..10} layers (seed 0), complex64: loss and full gradient of every
@@ -503,7 +592,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--case", default="gradient", choices=["gradient", "single-gate", "batched"])
+    ap.add_argument("--case", default="gradient", choices=["gradient", "single-gate", "batched", "lossy"])
     ap.add_argument("--circuits", type=int, default=4096)
     ap.add_argument("--only", default="", help="single-gate case: comma-separated subset of the kernels")
     ap.add_argument("--modes", type=int, default=7, help="single-gate case: modes of the cutoff-12 ket")
@@ -513,6 +602,8 @@ def main():
         return single_gate_case(args)
     if args.case == "batched":
         return batched_case(args)
+    if args.case == "lossy":
+        return lossy_case(args)
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
 

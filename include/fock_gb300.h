@@ -206,6 +206,16 @@ int fock_plan_forward(fock_plan* plan, const double* params, const void* state_i
 int fock_plan_backward(fock_plan* plan, const double* params, const void* state_in,
                        const void* states, int store_every, void* seg, void* grad_state, void* grad_tmp,
                        double* grad_params, void* workspace, void* stream);
+/* As fock_plan_backward, with `seg` holding only `seg_slots` states (at least
+ * 3 when seg_slots < store_every - 1): each checkpoint segment is then
+ * recomputed recursively -- chunk boundaries into seg slots through two
+ * scratch slots, every chunk processed the same way, last chunk first -- so
+ * the adjoint of a long segment (a density matrix of many GB between
+ * checkpoints) runs in bounded memory at the cost of extra forward passes. */
+int fock_plan_backward_recompute(fock_plan* plan, const double* params, const void* state_in,
+                                 const void* states, int store_every, void* seg, int seg_slots,
+                                 void* grad_state, void* grad_tmp, double* grad_params, void* workspace,
+                                 void* stream);
 
 /* Per-op device timing of plan sweeps (CUDA events recorded between the op
  * launches on the sweep's stream).  After enabling, every forward/backward

@@ -81,6 +81,7 @@ _SIGS = {
     "fock_plan_op": (_i, [_vp, _i, _ip, _ip, _ip, _ip]),
     "fock_plan_forward": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp]),
     "fock_plan_backward": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "fock_plan_backward_recompute": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp]),
     "fock_plan_enable_timing": (_i, [_vp, _i]),
     "fock_plan_op_times": (_i, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "fock_plan_sweep_status": (_i, [_vp, _vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),

@@ -47,10 +47,14 @@ class CompiledCircuit:
         pure (bool): ket ``[D]*n`` (default) or density matrix ``[D]*(2n)``
             with interleaved (ket, bra) axes; mixed circuits may contain
             ``LOSS`` gates (parameter T)
+        recompute_slots (int): states the backward sweep may hold while it
+            recomputes a checkpoint segment (default ``checkpoint - 1``: the
+            whole segment); fewer (at least 3) recompute the segment
+            recursively in bounded memory
     """
 
     def __init__(self, num_modes, cutoff, gates, n_params, dtype=torch.complex64, device=None, batch=1,
-                 checkpoint=1, pure=True):
+                 checkpoint=1, pure=True, recompute_slots=None):
         lib = L.load()
         self.num_modes = int(num_modes)
         self.cutoff = int(cutoff)
@@ -67,6 +71,7 @@ class CompiledCircuit:
         self.pure = bool(pure)
         if self.checkpoint < 1:
             raise ValueError("checkpoint must be >= 1")
+        self.recompute_slots = max(self.checkpoint - 1, 1) if recompute_slots is None else int(recompute_slots)
         L.check(lib.fock_plan_create_batch(self.num_modes, self.cutoff, 1 if self.pure else 0, self._dcode, arr,
                                            len(gates), self.n_params, self.batch, ctypes.byref(plan)),
                 "fock_plan_create")
@@ -164,11 +169,17 @@ class CompiledCircuit:
             return states[self.final_index(0)]
         return states
 
-    def backward(self, params, states, grad_state, state_in=None):
-        """Adjoint sweep: returns (dL/dparams, dL/dstate_in) given dL/dpsi_final."""
+    def backward(self, params, states, grad_state, state_in=None, overwrite_grad=False):
+        """Adjoint sweep: returns (dL/dparams, dL/dstate_in) given dL/dpsi_final.
+        With ``overwrite_grad`` a contiguous ``grad_state`` of the state dtype
+        is used as the sweep's buffer (and holds dL/dstate_in afterwards)
+        instead of a copy."""
         p = self._params(params)
         x = self._vacuum if state_in is None else state_in.to(self.dtype).contiguous()
-        lam = grad_state.to(self.dtype).contiguous().clone()
+        if overwrite_grad and grad_state.dtype == self.dtype and grad_state.is_contiguous():
+            lam = grad_state
+        else:
+            lam = grad_state.to(self.dtype).contiguous().clone()
         tmp = torch.empty_like(lam)
         grads = torch.empty(([self.batch] if self.batch > 1 else []) + [self.n_params], dtype=torch.float64,
                             device=self.device)
@@ -176,12 +187,13 @@ class CompiledCircuit:
             grads.zero_()
             return grads, lam
         k = self.checkpoint
-        seg = torch.empty([max(k - 1, 1)] + self._bshape, dtype=self.dtype, device=self.device) if k > 1 else None
-        L.check(L.load().fock_plan_backward(self._plan, p.data_ptr(), x.data_ptr(), states.data_ptr(), k,
-                                            seg.data_ptr() if seg is not None else None, lam.data_ptr(),
-                                            tmp.data_ptr(), grads.data_ptr(), self._ws.data_ptr(),
-                                            self._stream()),
-                "fock_plan_backward")
+        nslot = self.recompute_slots
+        seg = torch.empty([nslot] + self._bshape, dtype=self.dtype, device=self.device) if k > 1 else None
+        L.check(L.load().fock_plan_backward_recompute(self._plan, p.data_ptr(), x.data_ptr(), states.data_ptr(), k,
+                                                      seg.data_ptr() if seg is not None else None, nslot,
+                                                      lam.data_ptr(), tmp.data_ptr(), grads.data_ptr(),
+                                                      self._ws.data_ptr(), self._stream()),
+                "fock_plan_backward_recompute")
         return grads, lam
 
     def sweep_status(self):

@@ -670,14 +670,131 @@ static int param_grads(fock_plan* P, unsigned char* ws, const SweepCtx& c, doubl
   return FOCK_OK;
 }
 
+// one adjoint sweep in progress: lam holds dL/d(output of the next op to
+// process), other receives dL/d(its input)
+struct BwdCtx {
+  fock_plan* P;
+  SweepCtx c;
+  unsigned char* ws;
+  double2* cpart;
+  void* lam;
+  void* other;
+  int pdl;
+};
+
+static int adjoint_op(BwdCtx& b, int k, const void* psi_in) {
+  fock_plan* P = b.P;
+  const PlanOp& op = P->ops[k];
+  cudaStream_t st = b.c.st;
+  int rc;
+  if (P->timing && (rc = record_event(P->ev_bwd[k + 1], st))) return rc;
+  double2* cout = (double2*)(b.ws + P->o_carena) + op.c_off;
+  if (op.plane) {
+    rc = launch_plane_adjoint(P->dtype, psi_in, b.lam, b.other, op.pg_adj, op.grid_adj, b.c.arena + op.m_off,
+                              op_flags(op), b.cpart, st, b.c.bt);
+    if (rc) return rc;
+    rc = launch_reduce_partials(b.cpart, op.grid_adj, op.nent, cout, st, P->batch, P->cpart_entries,
+                                P->carena_entries, b.pdl);
+  } else {
+    rc = launch_adjoint_partials(P->dtype, psi_in, b.lam, b.other, op.view, P->D, op.layout, b.c.arena + op.m_off,
+                                 op_flags(op), b.cpart, op.sched, st, b.c.bt);
+    if (rc) return rc;
+    rc = launch_reduce_sched(b.cpart, op.sched, P->D, op.layout, cout, st, P->batch, P->cpart_entries,
+                             P->carena_entries, b.pdl);
+  }
+  if (rc) return rc;
+  b.c.bt.pdl = b.pdl;
+  std::swap(b.lam, b.other);
+  return FOCK_OK;
+}
+
+static int forward_op(BwdCtx& b, int j, const void* in, void* out) {
+  const int rc = apply_op(b.c, j, in, out);
+  b.c.bt.pdl = b.pdl;
+  return rc;
+}
+
+// Adjoint of ops [s0, e) whose first input is x, recomputing the states in
+// between into slots taken from `pool` (returned afterwards).
+//  - n - 1 <= F free slots: recompute the n - 1 inner states once, keep them.
+//  - otherwise split at m boundaries (recomputed through two scratch slots);
+//    chunk i is processed while boundaries 1..i are held, so it may keep up
+//    to F - i states: the last chunks take F - i + 1 ops, the first chunk the
+//    rest.  The fewest boundaries that cover the segment this way are used
+//    (one recomputation of the segment plus one of each chunk).
+//  - if no split covers it, one boundary F ops before the end: that chunk is
+//    processed directly, the front part again by this rule.
+static int bwd_range(BwdCtx& b, int s0, int e, const void* x, std::vector<void*>& pool) {
+  const int n = e - s0;
+  if (n <= 0) return FOCK_OK;
+  const int F = (int)pool.size();
+  int rc;
+  if (n - 1 <= F) {
+    std::vector<void*> sl(pool.end() - (n - 1), pool.end());
+    pool.resize(F - (n - 1));
+    const void* cur = x;
+    for (int j = s0; j < e - 1; ++j) {
+      if ((rc = forward_op(b, j, cur, sl[j - s0]))) return rc;
+      cur = sl[j - s0];
+    }
+    for (int k = e - 1; k >= s0; --k)
+      if ((rc = adjoint_op(b, k, k == s0 ? x : sl[k - s0 - 1]))) return rc;
+    pool.insert(pool.end(), sl.begin(), sl.end());
+    return FOCK_OK;
+  }
+  if (F < 3) return fock_set_error(FOCK_ERR_INVALID, "recomputing a segment of %d ops needs at least 3 slots", n);
+  int m = 0;
+  for (int t = 1; t <= F - 2 && t <= n - 1 && !m; ++t) {
+    int64_t cap = 0;
+    for (int i = 0; i <= t; ++i) cap += F - i + 1;
+    if (cap >= n) m = t;
+  }
+  std::vector<int> start;
+  if (m) {
+    start.assign(m + 2, 0);
+    start[0] = s0;
+    start[m + 1] = e;
+    for (int i = m; i >= 1; --i) start[i] = start[i + 1] - (F - i + 1);
+  } else {
+    m = 1;
+    start = {s0, e - F, e};
+  }
+  std::vector<void*> bound(m + 1, nullptr);
+  for (int i = 1; i <= m; ++i) { bound[i] = pool.back(); pool.pop_back(); }
+  void* scratch[2] = {pool[pool.size() - 1], pool[pool.size() - 2]};
+  const void* cur = x;
+  int nb = 1;  // next boundary to fill
+  for (int j = s0; j < start[m]; ++j) {
+    void* dst = (j + 1 == start[nb]) ? bound[nb] : scratch[j & 1];
+    if ((rc = forward_op(b, j, cur, dst))) return rc;
+    if (j + 1 == start[nb]) ++nb;
+    cur = dst;
+  }
+  for (int i = m; i >= 0; --i) {
+    if ((rc = bwd_range(b, start[i], start[i + 1], i == 0 ? x : bound[i], pool))) return rc;
+    if (i >= 1) pool.push_back(bound[i]);
+  }
+  return FOCK_OK;
+}
+
 extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void* state_in,
                                   const void* states, int store_every, void* seg, void* grad_state,
                                   void* grad_tmp, double* grad_params, void* workspace, void* stream) {
+  return fock_plan_backward_recompute(P, params, state_in, states, store_every, seg,
+                                      store_every > 1 ? store_every - 1 : 0, grad_state, grad_tmp, grad_params,
+                                      workspace, stream);
+}
+
+extern "C" int fock_plan_backward_recompute(fock_plan* P, const double* params, const void* state_in,
+                                            const void* states, int store_every, void* seg, int seg_slots,
+                                            void* grad_state, void* grad_tmp, double* grad_params,
+                                            void* workspace, void* stream) {
   if (!P) return fock_set_error(FOCK_ERR_INVALID, "null plan");
   if (!state_in || !states || !grad_state || !grad_tmp || !workspace)
     return fock_set_error(FOCK_ERR_INVALID, "null buffer");
   if (store_every < 1) return fock_set_error(FOCK_ERR_INVALID, "the adjoint sweep needs store_every >= 1");
-  if (store_every > 1 && !seg) return fock_set_error(FOCK_ERR_INVALID, "checkpointed sweep needs a segment buffer");
+  if (store_every > 1 && (!seg || seg_slots < 1))
+    return fock_set_error(FOCK_ERR_INVALID, "checkpointed sweep needs a segment buffer");
   if (P->n_params > 0 && (!params || !grad_params)) return fock_set_error(FOCK_ERR_INVALID, "null parameter array");
   cudaStream_t st = (cudaStream_t)stream;
   unsigned char* ws = (unsigned char*)workspace;
@@ -685,11 +802,8 @@ extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void
   if (rc) return rc;
   SweepCtx c;
   sweep_ctx(P, ws, st, &c);
-  double2* cpart = (double2*)(ws + P->o_cpart);
   const int n_ops = (int)P->ops.size();
   const int K = store_every;
-  void* lam = grad_state;
-  void* other = grad_tmp;
   if (P->persist && !P->timing && K == 1 && n_ops > 0) {
     SweepSync sync;
     if ((rc = sweep_sync(P, ws, st, &sync))) return rc;
@@ -707,60 +821,37 @@ extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void
     if ((rc = ensure_events(P->ev_bwd, n_ops + 1))) return rc;
     P->bwd_recorded = 0;
   }
-  const int nseg = K == 1 ? 1 : (n_ops + K - 1) / K;
+  BwdCtx b;
+  b.P = P;
+  b.c = c;
+  b.ws = ws;
+  b.cpart = (double2*)(ws + P->o_cpart);
+  b.lam = grad_state;
+  b.other = grad_tmp;
   // programmatic dependent launch for every sweep kernel but the first one
   // after the matrix build (and none around timing events)
-  const int pdl = !P->timing;
-  c.bt.pdl = 0;
-  for (int sgi = nseg - 1; sgi >= 0; --sgi) {
-    const int s0 = K == 1 ? 0 : sgi * K;
-    const int e = K == 1 ? n_ops : std::min(s0 + K, n_ops);
-    const void* seg_in = state_in;
-    if (K > 1) {
-      // recompute the segment's inner states from its checkpoint
-      seg_in = sgi == 0 ? state_in : (const char*)states + (int64_t)(sgi - 1) * c.sb;
-      const void* cur = seg_in;
-      for (int j = s0; j < e - 1; ++j) {
-        void* dst = (char*)seg + (int64_t)(j - s0) * c.sb;
-        if ((rc = apply_op(c, j, cur, dst))) return rc;
-        c.bt.pdl = pdl;
-        cur = dst;
-      }
-    }
-    for (int k = e - 1; k >= s0; --k) {
-      const PlanOp& op = P->ops[k];
-      const void* psi_in;
-      if (K == 1) psi_in = k == 0 ? state_in : (const char*)states + (int64_t)(k - 1) * c.sb;
-      else psi_in = k == s0 ? seg_in : (const char*)seg + (int64_t)(k - s0 - 1) * c.sb;
-      if (P->timing && (rc = record_event(P->ev_bwd[k + 1], st))) return rc;
-      double2* cout = (double2*)(ws + P->o_carena) + op.c_off;
-      if (op.plane) {
-        rc = launch_plane_adjoint(P->dtype, psi_in, lam, other, op.pg_adj, op.grid_adj, c.arena + op.m_off,
-                                  op_flags(op), cpart, st, c.bt);
-        if (rc) return rc;
-        rc = launch_reduce_partials(cpart, op.grid_adj, op.nent, cout, st, P->batch, P->cpart_entries,
-                                    P->carena_entries, pdl);
-      } else {
-        rc = launch_adjoint_partials(P->dtype, psi_in, lam, other, op.view, P->D, op.layout, c.arena + op.m_off,
-                                     op_flags(op), cpart, op.sched, st, c.bt);
-        if (rc) return rc;
-        rc = launch_reduce_sched(cpart, op.sched, P->D, op.layout, cout, st, P->batch, P->cpart_entries,
-                                 P->carena_entries, pdl);
-      }
-      if (rc) return rc;
-      c.bt.pdl = pdl;
-      void* t = lam;
-      lam = other;
-      other = t;
+  b.pdl = !P->timing;
+  b.c.bt.pdl = 0;
+  if (K == 1) {
+    for (int k = n_ops - 1; k >= 0; --k)
+      if ((rc = adjoint_op(b, k, k == 0 ? state_in : (const char*)states + (int64_t)(k - 1) * c.sb))) return rc;
+  } else {
+    std::vector<void*> pool;
+    for (int i = seg_slots - 1; i >= 0; --i) pool.push_back((char*)seg + (int64_t)i * c.sb);
+    const int nseg = (n_ops + K - 1) / K;
+    for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+      const int s0 = sgi * K, e = std::min(s0 + K, n_ops);
+      const void* seg_in = sgi == 0 ? state_in : (const char*)states + (int64_t)(sgi - 1) * c.sb;
+      if ((rc = bwd_range(b, s0, e, seg_in, pool))) return rc;
     }
   }
+  void* lam = b.lam;
   if (P->timing) {
     if ((rc = record_event(P->ev_bwd[0], st))) return rc;
     P->bwd_recorded = 1;
   }
   if (lam != grad_state) FOCK_CUDA_TRY(cudaMemcpyAsync(grad_state, lam, c.sb, cudaMemcpyDeviceToDevice, st));
   return param_grads(P, ws, c, grad_params, st);
-  return FOCK_OK;
 }
 
 extern "C" int fock_plan_sweep_status(const fock_plan* P, const void* workspace, int* grids, int* error) {

@@ -52,7 +52,22 @@ def qnn_gates(N, layers):
     return gates, p
 
 
-def qnn_params(gates, n_params, seed, r_max=0.3, a_max=0.3, k_max=0.05):
+def lossy_qnn_gates(N, layers):
+    """``qnn_gates`` with a loss channel on every mode at the end of every
+    layer (the mixed-state lossy workload: LossChannel(T) per mode per layer,
+    reference ops.py LossChannel / fockbackend/circuit.py:65-87)."""
+    gates, p = [], 0
+    for _ in range(layers):
+        layer, n = qnn_gates(N, 1)
+        gates += [(k, m1, m2, pi + p) for k, m1, m2, pi in layer]
+        p += n
+        for m in range(N):
+            gates.append((L.LOSS, m, -1, p))
+            p += 1
+    return gates, p
+
+
+def qnn_params(gates, n_params, seed, r_max=0.3, a_max=0.3, k_max=0.05, t_min=0.8):
     """Seeded parameter vector for a ``qnn_gates`` list."""
     rng = np.random.default_rng(seed)
     p = np.zeros(n_params)
@@ -70,6 +85,8 @@ def qnn_params(gates, n_params, seed, r_max=0.3, a_max=0.3, k_max=0.05):
             p[i + 1] = rng.uniform(0, 2 * np.pi)
         elif kind == L.KERR:
             p[i] = rng.uniform(0, k_max)
+        elif kind == L.LOSS:
+            p[i] = rng.uniform(t_min, 1.0)
     return p
 
 

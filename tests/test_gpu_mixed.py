@@ -127,3 +127,37 @@ def test_mixed_gradient_c64_and_checkpoints(cuda):
     assert np.linalg.norm(g64 - g128) <= 1e-4 * np.linalg.norm(g128)
     gk, _ = _grad(_circuit(N, D, gates, len(params), torch.complex128, checkpoint=3), params, w, N, cuda)
     assert np.linalg.norm(gk - g128) <= 1e-12 * np.linalg.norm(g128)
+
+
+@pytest.mark.parametrize("k,slots", [(1000, 3), (1000, 4), (1000, 7), (9, 3), (9, 5), (9, 8)])
+def test_recursive_recompute_matches_stored_states(cuda, k, slots):
+    """A checkpoint segment recomputed recursively in `slots` states gives the
+    same gradient as keeping every state (same kernels on the same inputs)."""
+    N, D = 3, 5
+    gates, params = _random_mixed(N, 4)
+    w = _weights(N, D, 3)
+    g1, l1 = _grad(_circuit(N, D, gates, len(params), torch.complex128), params, w, N, cuda)
+    gk, lk = _grad(_circuit(N, D, gates, len(params), torch.complex128, checkpoint=k, recompute_slots=slots),
+                   params, w, N, cuda)
+    assert lk == l1
+    np.testing.assert_allclose(gk, g1, rtol=1e-13, atol=1e-15)
+
+
+def test_recursive_recompute_pure_qnn(cuda):
+    from strawberryfields_gb300 import CompiledCircuit
+    from strawberryfields_gb300.qnn import qnn_gates, qnn_params
+
+    gates, npar = qnn_gates(3, 3)
+    params = qnn_params(gates, npar, seed=2)
+    t = torch.randn(7, 7, 7, dtype=torch.complex64, device=cuda)
+
+    def grad(circ):
+        p = torch.tensor(params, device=cuda, requires_grad=True)
+        psi = circ(p)
+        loss = torch.abs(torch.sum(t.conj() * psi)) ** 2
+        loss.backward()
+        return p.grad.detach().cpu().numpy()
+
+    g1 = grad(CompiledCircuit(3, 7, gates, npar, dtype=torch.complex64, device=cuda))
+    g2 = grad(CompiledCircuit(3, 7, gates, npar, dtype=torch.complex64, device=cuda, checkpoint=20, recompute_slots=4))
+    np.testing.assert_allclose(g2, g1, rtol=1e-6, atol=1e-9)
