@@ -65,6 +65,18 @@ class CircuitBatch:
                                    checkpoint=k)
             self.groups.append({"key": key, "idx": np.array(idx), "circ": circ, "n_ops": n_ops})
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max(1, streams))]
+        # flat parameter layout: circuit order, and the same entries group by group
+        npar = [int(c[3]) for c in circuits]
+        self.param_offsets = np.concatenate([[0], np.cumsum(npar)]).astype(np.int64)
+        order = []
+        for g in self.groups:
+            for i in g["idx"]:
+                order.extend(range(self.param_offsets[i], self.param_offsets[i + 1]))
+        self._gather = torch.as_tensor(np.array(order, dtype=np.int64), device=self.device)
+        # circuit index of every loss in group order
+        self._order = torch.as_tensor(np.concatenate([g["idx"] for g in self.groups]).astype(np.int64),
+                                      device=self.device)
+        self.graph = None
 
     def stats(self):
         """Groups, fused ops and algorithmic bytes of one forward + adjoint."""
@@ -120,6 +132,79 @@ class CircuitBatch:
         for st in self.streams:
             cur.wait_stream(st)
         return losses, grads
+
+
+    def _group_params(self, flat_group):
+        """Per-group parameter views ([batch, n_params]) of a group-ordered
+        flat vector."""
+        out, o = [], 0
+        for g in self.groups:
+            nb, npar = len(g["idx"]), g["key"][3]
+            out.append(flat_group[o:o + nb * npar].view(nb, npar) if nb > 1 else flat_group[o:o + npar])
+            o += nb * npar
+        return out
+
+    def _step(self, flat_params, targets, losses, grads):
+        """One step on group-ordered views: every group's forward, loss and
+        adjoint, results scattered into losses [n] and grads (flat, circuit
+        order)."""
+        flat_group = flat_params.index_select(0, self._gather)
+        gparams = self._group_params(flat_group)
+        cur = torch.cuda.current_stream(self.device)
+        gl, gg = [], []
+        for gi, g in enumerate(self.groups):
+            st = self.streams[gi % len(self.streams)]
+            st.wait_stream(cur)
+            with torch.cuda.stream(st):
+                circ, idx = g["circ"], g["idx"]
+                p = gparams[gi]
+                states = circ.forward_states(p)
+                psi = states[circ.final_index()]
+                t = targets[(g["key"][0], g["key"][1])].to(circ.dtype)
+                if len(idx) > 1:
+                    loss, gpsi = fidelity_loss_grad(psi, t.unsqueeze(0).expand_as(psi))
+                else:
+                    loss, gpsi = fidelity_loss_grad(psi.unsqueeze(0), t.unsqueeze(0))
+                    gpsi = gpsi[0]
+                gr, _ = circ.backward(p, states, gpsi)
+                del states, psi, gpsi
+                circ.release()
+                gl.append(loss.reshape(-1))
+                gg.append(gr.reshape(-1))
+        for st in self.streams:
+            cur.wait_stream(st)
+        losses.index_copy_(0, self._order, torch.cat(gl).to(losses.dtype))
+        grads.index_copy_(0, self._gather, torch.cat(gg))
+
+    def capture(self, params, targets, warmup=1):
+        """Capture one whole step -- every group's forward sweep, loss and
+        adjoint sweep on the group streams -- as a single CUDA graph.  Returns
+        ``step(flat_params=None) -> (losses [n], grads flat)``; parameters are
+        a flat circuit-order vector (``param_offsets`` per circuit) copied into
+        the graph's input buffer before each replay."""
+        flat = torch.cat([torch.as_tensor(p, device=self.device, dtype=torch.float64).reshape(-1) for p in params])
+        self._in = flat.clone()
+        self._losses = torch.zeros(self.n, dtype=torch.float64, device=self.device)
+        self._grads = torch.zeros_like(flat)
+        cur = torch.cuda.current_stream(self.device)
+        side = torch.cuda.Stream(device=self.device)
+        side.wait_stream(cur)
+        with torch.cuda.stream(side):
+            for _ in range(warmup):
+                self._step(self._in, targets, self._losses, self._grads)
+        cur.wait_stream(side)
+        torch.cuda.synchronize(self.device)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._step(self._in, targets, self._losses, self._grads)
+
+        def step(flat_params=None):
+            if flat_params is not None:
+                self._in.copy_(flat_params, non_blocking=True)
+            self.graph.replay()
+            return self._losses, self._grads
+
+        return step
 
 
 def random_qnn_batch(n_circuits, seed=0, modes=(2, 5), cutoffs=(6, 20), depths=(2, 10)):

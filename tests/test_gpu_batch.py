@@ -34,3 +34,30 @@ def test_heterogeneous_batch_matches_oracle(cuda, dtype):
         ref = fo.adjoint_grads(gates, params[i], nm, D, -2 * s * t)
         rel = np.linalg.norm(grads[i].cpu().numpy() - ref) / max(np.linalg.norm(ref), 1e-30)
         assert rel < (1e-10 if dtype == "complex128" else 1e-5), (i, rel)
+
+
+def test_captured_batch_step_matches_eager(cuda):
+    """The whole heterogeneous step captured as one CUDA graph (every group's
+    forward, loss and adjoint on the group streams) reproduces the eager step
+    and follows new parameters copied into its input buffer."""
+    import torch
+    from strawberryfields_gb300.batch import CircuitBatch, random_qnn_batch
+    from strawberryfields_gb300.qnn import target_state
+
+    circuits, params = random_qnn_batch(12, seed=4, modes=(2, 3), cutoffs=(4, 6), depths=(1, 2))
+    cb = CircuitBatch(circuits, dtype=torch.complex128, streams=3, checkpoint_bytes=20_000)
+    targets = {(nm, D): torch.as_tensor(target_state(nm, D, 2, seed=nm * 100 + D), device="cuda")
+               for nm, D, _, _ in circuits}
+    pt = [torch.tensor(p, device="cuda") for p in params]
+    step = cb.capture(pt, targets)
+    for scale in (1.0, 0.7):
+        pts = [p * scale for p in pt]
+        losses, grads = step(torch.cat(pts))
+        l_e, g_e = cb.value_and_grad(pts, targets)
+        torch.cuda.synchronize()
+        assert torch.allclose(losses, torch.stack([x.reshape(()) for x in l_e]).to(losses.dtype), atol=1e-12)
+        ge = torch.cat([g.reshape(-1) for g in g_e])
+        assert torch.allclose(grads, ge, atol=1e-12, rtol=1e-12)
+        for i in range(len(circuits)):
+            o0, o1 = cb.param_offsets[i], cb.param_offsets[i + 1]
+            assert torch.allclose(grads[o0:o1], g_e[i].reshape(-1), atol=1e-12)
