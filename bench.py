@@ -186,11 +186,18 @@ def _peaks():
 
 
 def _traffic():
-    try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            return json.load(f)
-    except (OSError, ValueError):
-        return {}
+    """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum)
+    of a kernel class from the committed ncu summaries: lines
+    'traffic_bytes_per_launch <class> = <bytes>'."""
+    import glob
+    import re
+
+    out = {}
+    for fn in glob.glob(os.path.join(ROOT, "profiles", "*.md")):
+        with open(fn) as f:
+            for m in re.finditer(r"^traffic_bytes_per_launch (\S+) = (\d+)", f.read(), re.M):
+                out[m.group(1)] = int(m.group(2))
+    return out
 
 
 def gpu_arm(args, rank, world, cpu_base):
