@@ -518,6 +518,50 @@ def run_gates(gates, params, N, D, state=None):
     return out
 
 
+def homodyne_pdf(rho, phi, hbar=2.0, q_max=10.0, num_bins=100000):
+    """Binned distribution of the quadrature x cos(phi) + p sin(phi) of a
+    single-mode density matrix ``rho`` (reference fockbackend/circuit.py
+    :724-755): rho rotated by R(-phi), physicists' Hermite polynomials by
+    their recurrence, pdf times the bin width.  Returns (grid, probabilities)."""
+    D = rho.shape[0]
+    mw = 1.0 / hbar
+    n = np.arange(D)
+    U = np.diag(np.exp(-1j * phi * n))
+    r = U @ rho @ U.conj().T
+    q = np.linspace(-q_max, q_max, num_bins)
+    x = np.sqrt(mw) * q
+    H = [np.ones_like(x), 2 * x]
+    for k in range(2, D):
+        H.append(2 * x * H[k - 1] - 2 * (k - 1) * H[k - 2])
+    dist = np.zeros(num_bins, dtype=CDT)
+    for a in range(D):
+        for b in range(D):
+            dist += r[a, b] * H[a] * H[b] / math.sqrt(2 ** a * math.factorial(a) * 2 ** b * math.factorial(b))
+    return q, (dist * np.sqrt(mw / np.pi) * np.exp(-mw * q ** 2) * (q[1] - q[0])).real
+
+
+def homodyne_project(state, phi, x, mode, n, pure=True, hbar=2.0):
+    """State after a homodyne outcome ``x`` on ``mode`` (reference
+    circuit.py:766-795): |0><x_phi| applied to the mode, with x_phi =
+    R(phi) D(alpha) times the truncated infinitely squeezed vacuum, alpha =
+    x sqrt(1 / (2 hbar)); renormalised (2-norm for a ket, trace for a
+    density matrix)."""
+    D = state.shape[0]
+    sq = np.array([(-0.5) ** (k // 2) * math.sqrt(math.factorial(k)) / math.factorial(k // 2) if k % 2 == 0 else 0.0
+                   for k in range(D)], dtype=CDT)
+    alpha = x * math.sqrt(1.0 / (2 * hbar))
+    eig = phase(phi, D) @ displacement(abs(alpha), np.angle(alpha), D) @ sq
+    P = np.zeros((D, D), dtype=CDT)
+    P[0, :] = eig.conj()
+    out = apply_gate1(state, P, mode, pure)
+    if pure:
+        return out / np.linalg.norm(out)
+    tr = np.real(np.trace(out.reshape(D ** n, D ** n) if n == 1 else
+                          np.transpose(out, [2 * i for i in range(n)] + [2 * i + 1 for i in range(n)])
+                          .reshape(D ** n, D ** n)))
+    return out / tr
+
+
 def run_gates_mixed(gates, params, N, D, rho=None):
     """Density-matrix run of a gate list (vacuum by default): unitaries as
     ``U rho U^dag`` (reference circuit.py:186-217), ``LOSS`` (parameter T) as

@@ -214,7 +214,15 @@ class FockGB300Backend:
         return self.circuit.measure_fock(self._remap_modes(modes), select=select)
 
     def measure_homodyne(self, phi, mode, shots=1, select=None, **kwargs):
-        raise NotImplementedError("fock_gb300 backend does not implement homodyne measurement yet")
+        """Homodyne measurement (reference fockbackend/backend.py:184-198).
+
+        Keyword Args:
+            num_bins (int): bins of the sampled distribution (default 100000)
+            max (float): the distribution is binned on [-max, max] (default 10)
+        """
+        if shots != 1:
+            raise NotImplementedError("fock backend currently does not support shots != 1 for homodyne measurement")
+        return self.circuit.measure_homodyne(phi, self._remap_modes(mode), select=select, **kwargs)
 
     def is_vacuum(self, tol=0.0, **kwargs):
         return self.circuit.is_vacuum(tol)

@@ -10,6 +10,7 @@ pass before any readout -- the state crosses HBM once per gate group.
 """
 
 import math
+import numbers
 
 import numpy as np
 import torch
@@ -416,6 +417,71 @@ class DeviceCircuit:
         else:
             self._state = self._state / nrm
         return np.array([outcome])
+
+    def homodyne_pdf(self, phi, mode, q_max=10.0, num_bins=100000):
+        """Quadrature distribution of x_phi on ``mode`` on the grid
+        ``linspace(-q_max, q_max, num_bins)``, as probabilities per bin (the
+        pdf times the bin width; reference circuit.py:734-755): from the mode's
+        reduced density matrix rotated by R(-phi), with the Hermite functions
+        h_n = H_n / sqrt(2^n n!) by their normalised recurrence.  Returns
+        (grid, probabilities) as float64 device tensors."""
+        D = self._trunc
+        mw = 1.0 / self._hbar
+        rho = self.reduced_dm1(mode)
+        n = torch.arange(D, dtype=torch.float64, device=self._device)
+        ph = torch.exp(-1j * phi * n)
+        rho = ph[:, None] * rho * ph.conj()[None, :]
+        q = torch.linspace(-q_max, q_max, num_bins, dtype=torch.float64, device=self._device)
+        x = math.sqrt(mw) * q
+        h = torch.empty((D, num_bins), dtype=torch.float64, device=self._device)
+        h[0] = 1.0
+        if D > 1:
+            h[1] = math.sqrt(2.0) * x
+        for k in range(2, D):
+            h[k] = math.sqrt(2.0 / k) * x * h[k - 1] - math.sqrt((k - 1) / k) * h[k - 2]
+        hc = h.to(torch.complex128)
+        dist = torch.sum((rho @ hc) * hc, dim=0).real
+        dist = dist * math.sqrt(mw / math.pi) * torch.exp(-mw * q * q) * (q[1] - q[0])
+        return q, dist
+
+    def measure_homodyne(self, phi, mode, select=None, rng=None, **kwargs):
+        """Homodyne measurement of the quadrature x cos(phi) + p sin(phi) of
+        ``mode`` (reference circuit.py:713-801): one sample from the binned
+        distribution (``num_bins`` points in [-``max``, ``max``]), or the
+        post-selected value ``select``; the mode is then projected with
+        |0><x_phi| (x_phi the finite-cutoff quadrature eigenstate
+        R(phi) D(alpha) times the infinitely squeezed vacuum) and the state
+        renormalised.  Returns [[x]]."""
+        D = self._trunc
+        mw = 1.0 / self._hbar
+        if select is not None:
+            if not isinstance(select, numbers.Number):
+                raise TypeError("Selected measurement result must be of numeric type.")
+            sample = float(select)
+        else:
+            q, dist = self.homodyne_pdf(phi, mode, kwargs.get("max", 10), kwargs.get("num_bins", 100000))
+            probs = dist.cpu().numpy()
+            probs = probs / probs.sum()
+            probs[np.abs(probs) < 1e-10] = 0
+            rng = rng or np.random
+            idx = int(np.argmax(rng.multinomial(1, probs / probs.sum())))
+            sample = float(q[idx].item())
+        # |x_phi> in the truncated Fock basis
+        sq = np.zeros(D, dtype=np.complex128)
+        for k in range(0, D, 2):
+            sq[k] = (-0.5) ** (k // 2) * math.sqrt(math.factorial(k)) / math.factorial(k // 2)
+        alpha = sample * math.sqrt(mw / 2)
+        disp = self.gate_matrix(L.DISPLACEMENT, abs(alpha), float(np.angle(alpha))).cpu().numpy()
+        rot = np.exp(1j * phi * np.arange(D))
+        eig = (rot[:, None] * disp) @ sq
+        P = np.zeros((D, D), dtype=np.complex128)
+        P[0, :] = eig.conj()
+        self.apply_matrix(P, mode)
+        nrm = self.norm()
+        if nrm == 0:
+            raise ZeroDivisionError("Measurement has zero probability.")
+        self._state = self._state / nrm
+        return np.array([[sample]])
 
     def _project_reset(self, modes, values):
         """Apply |0><x| on each measured mode (reference ops.py:180-205)."""

@@ -13,6 +13,9 @@ oracle's FP64 restatement) on seeded circuits and stores inputs and outputs:
   two-mode squeezer, MZ, cross-Kerr and loss channels.
 * ``pure_all_seed0``: 3 modes, cutoff 7, every pure gate kind incl. swapped
   and non-adjacent mode pairs with mode2 != 0.
+* ``homodyne_{pure,mixed}_seed0``: gates, a homodyne measurement with a
+  post-selected value ("MH": phi, value, mode; circuit.py:713-801 without the
+  sampling), then more gates.
 * ``swapped_mixed_seed0``: the same kinds with mode pairs (2, 0) and (1, 0),
   run on a mixed state.  The reference's pure-state two-mode path
   (fockbackend/circuit.py:242-248) moves the wrong axes to the front when
@@ -32,7 +35,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from oracle import sfref  # noqa: E402
 
 # op codes stored in the fixtures: (name, params..., modes...)
-OPS = {"S": 1, "D": 2, "BS": 3, "R": 4, "K": 5, "S2": 6, "MZ": 7, "CK": 8, "L": 9}
+OPS = {"S": 1, "D": 2, "BS": 3, "R": 4, "K": 5, "S2": 6, "MZ": 7, "CK": 8, "L": 9, "MH": 10}
 
 
 def cfg1(seed):
@@ -78,6 +81,16 @@ def swapped_mixed(seed):
     return 3, 5, False, ops
 
 
+def homodyne(seed, pure):
+    rng = np.random.default_rng(400 + seed + (0 if pure else 50))
+    u = rng.uniform
+    ops = [("S", u(0, .4), u(0, 6.28), 0), ("D", u(0, .5), u(0, 6.28), 1), ("BS", u(0, 1.5), u(0, 6.28), 0, 1)]
+    if not pure:
+        ops.append(("L", u(.7, 1), 1))
+    ops += [("MH", u(0, 6.28), u(-1.5, 1.5), 0), ("D", u(0, .4), u(0, 6.28), 0), ("BS", u(0, 1.5), u(0, 6.28), 0, 1)]
+    return 2, 8 if pure else 6, pure, ops
+
+
 def run_reference(N, D, pure, ops):
     _, Circuit = sfref.load_fock_circuit()
     c = Circuit(N, D, pure=pure)
@@ -101,6 +114,8 @@ def run_reference(N, D, pure, ops):
             c.cross_kerr_interaction(rest[0], rest[1], rest[2])
         elif name == "L":
             c.loss(rest[0], rest[1])
+        elif name == "MH":
+            c.measure_homodyne(rest[0], rest[2], select=rest[1])
     state, is_pure = c.get_state()
     return np.asarray(state, dtype=np.complex128), is_pure
 
@@ -110,7 +125,7 @@ def encode(ops):
     rows = []
     for op in ops:
         name = op[0]
-        if name in ("S", "D", "BS", "S2", "MZ"):
+        if name in ("S", "D", "BS", "S2", "MZ", "MH"):
             p = op[1:3]
             modes = op[3:]
         else:
@@ -138,6 +153,8 @@ def main():
     for s in range(2):
         cases[f"mixed_seed{s}"] = mixed(s)
     cases["pure_all_seed0"] = pure_all(0)
+    cases["homodyne_pure_seed0"] = homodyne(0, True)
+    cases["homodyne_mixed_seed0"] = homodyne(0, False)
     cases["swapped_mixed_seed0"] = swapped_mixed(0)
     for name, (N, D, pure, ops) in cases.items():
         state, is_pure = run_reference(N, D, pure, ops)

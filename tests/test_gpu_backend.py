@@ -266,3 +266,39 @@ def test_engine_integration(cuda):
     st = eng.run(prog).state
     ref, _ = _oracle_sequence(SEQ[:6], 3, 6, True)
     assert np.abs(st.ket() - ref).max() < TOL
+
+
+@pytest.mark.parametrize("pure", [True, False])
+def test_homodyne_distribution_and_sample(cuda, pure):
+    from strawberryfields_gb300.circuit import DeviceCircuit
+
+    D = 10
+    c = DeviceCircuit(2, D, pure=pure)
+    c.squeeze(0.3, 0.7, 0)
+    c.displacement(0.8, 0.4, 0)
+    c.beamsplitter(0.6, 0.2, 0, 1)
+    if not pure:
+        c.loss(0.8, 0)
+    rho = c.reduced_dm1(0).cpu().numpy()
+    q, got = c.homodyne_pdf(0.9, 0, q_max=8, num_bins=4001)
+    qr, ref = fo.homodyne_pdf(rho, 0.9, 2.0, 8, 4001)
+    assert np.abs(got.cpu().numpy() - ref).max() < 1e-12
+    # a sample, then mode 0 is in vacuum and the state normalised
+    x = c.measure_homodyne(0.9, 0, rng=np.random.RandomState(5), num_bins=4001, max=8)
+    assert x.shape == (1, 1) and -8 <= x[0, 0] <= 8
+    marg = c.marginals().cpu().numpy()
+    assert abs(marg[0, 0] - 1) < 1e-12 and abs(marg[1].sum() - 1) < 1e-12
+
+
+def test_homodyne_coherent_state_moments(cuda):
+    """|alpha> measured along phi = 0: mean sqrt(2 hbar) Re(alpha), variance hbar / 2."""
+    from strawberryfields_gb300.circuit import DeviceCircuit
+
+    c = DeviceCircuit(1, 20, pure=True)
+    c.displacement(0.7, 0.3, 0)
+    q, p = c.homodyne_pdf(0.0, 0, q_max=10, num_bins=20001)
+    q, p = q.cpu().numpy(), p.cpu().numpy()
+    mean = np.sum(q * p) / np.sum(p)
+    var = np.sum(q * q * p) / np.sum(p) - mean ** 2
+    assert abs(mean - 2 * 0.7 * np.cos(0.3)) < 1e-6
+    assert abs(var - 1.0) < 1e-6

@@ -19,7 +19,8 @@ def run_backend(N, D, pure, ops, dtype):
     b = FockGB300Backend()
     b.begin_circuit(N, cutoff_dim=D, pure=pure, dtype=dtype)
     table = {"S": b.squeeze, "D": b.displacement, "R": b.rotation, "K": b.kerr_interaction, "BS": b.beamsplitter,
-             "S2": b.two_mode_squeeze, "MZ": b.mzgate, "CK": b.cross_kerr_interaction, "L": b.loss}
+             "S2": b.two_mode_squeeze, "MZ": b.mzgate, "CK": b.cross_kerr_interaction, "L": b.loss,
+             "MH": lambda phi, x, m: b.measure_homodyne(phi, m, select=x)}
     for op in ops:
         table[op[0]](*op[1:])
     st = b.state()

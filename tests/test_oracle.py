@@ -152,6 +152,8 @@ def oracle_run(N, D, pure, ops):
         elif name == "L":
             s = fo.apply_loss(s, rest[0], rest[1], N, pure)
             pure = False
+        elif name == "MH":
+            s = fo.homodyne_project(s, rest[0], rest[1], rest[2], N, pure)
     return s
 
 
@@ -192,10 +194,26 @@ def test_oracle_mixed_gate_list_matches_golden():
         if not f.endswith(".npz"):
             continue
         z = np.load(os.path.join(golden, f))
-        if bool(z["pure"]):
+        if bool(z["pure"]) or np.any(z["ops"][:, 0] == 10):  # gate lists only (10: homodyne)
             continue
         gates, params = ops_to_gates(decode(z["ops"]))
         rho = fo.run_gates_mixed(gates, params, int(z["N"]), int(z["D"]))
         assert np.abs(rho - z["state"]).max() < 1e-12, f
         n += 1
     assert n >= 2
+
+
+def test_oracle_homodyne_pdf_coherent_state():
+    """The restated homodyne distribution of |alpha> along phi: a normal
+    distribution with mean sqrt(2 hbar) |alpha| cos(arg alpha - phi) and
+    variance hbar / 2 (hbar = 2)."""
+    D = 24
+    psi = fo.coherent_state(0.8, 0.5, D)
+    rho = np.outer(psi, psi.conj())
+    for phi in (0.0, 0.9):
+        q, p = fo.homodyne_pdf(rho, phi, 2.0, 10, 20001)
+        mean = np.sum(q * p) / np.sum(p)
+        var = np.sum(q * q * p) / np.sum(p) - mean ** 2
+        assert abs(np.sum(p) - 1) < 1e-6
+        assert abs(mean - 2 * 0.8 * np.cos(0.5 - phi)) < 1e-8
+        assert abs(var - 1.0) < 1e-8
