@@ -261,3 +261,65 @@ int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* 
   return FOCK_OK;
 }
 
+
+// every op's partial sums at once (one warp per C entry, lanes over the
+// op's CTAs, fixed order)
+__global__ void reduce_ops_kernel(const RedOp* __restrict__ ops, int n_ops, int64_t total, int D,
+                                  const double2* __restrict__ cpart, double2* __restrict__ carena,
+                                  int64_t part_stride, int64_t out_stride) {
+  pdl_wait();
+  pdl_launch_dependents();
+  const int lane = threadIdx.x & 31;
+  const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  cpart += blockIdx.y * part_stride;
+  carena += blockIdx.y * out_stride;
+  if (e >= total) return;
+  int lo = 0, hi = n_ops - 1;
+  while (lo < hi) {  // last op with c_off <= e
+    const int mid = (lo + hi + 1) >> 1;
+    if (ops[mid].c_off <= e) lo = mid;
+    else hi = mid - 1;
+  }
+  const RedOp R = ops[lo];
+  const int64_t le = e - R.c_off;
+  const double2* src;
+  int64_t stride;
+  if (R.plane) {
+    src = cpart + R.cpart_off + le;
+    stride = R.nent;
+  } else if (R.layout == LAYOUT_DENSE) {
+    src = cpart + R.cpart_off + le;
+    stride = (int64_t)D * D;
+  } else {
+    int bs = 0, s = 1;
+    int64_t off = 0;
+    for (bs = 0; bs < 2 * D - 1; ++bs) {
+      s = blk_size(D, bs);
+      if (le < off + (int64_t)s * s) break;
+      off += (int64_t)s * s;
+    }
+    src = cpart + R.cpart_off + (int64_t)R.gx * off + (le - off);
+    stride = (int64_t)s * s;
+  }
+  double2 a = make_double2(0.0, 0.0);
+  for (int x = lane; x < R.gx; x += 32) {
+    const double2 p = src[(int64_t)x * stride];
+    a.x += p.x;
+    a.y += p.y;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
+    a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
+  }
+  if (lane == 0) carena[e] = a;
+}
+
+int launch_reduce_ops(const RedOp* ops, int n_ops, int64_t total, int D, const double2* cpart, double2* carena,
+                      cudaStream_t st, int nb, int64_t part_stride, int64_t out_stride) {
+  if (total <= 0) return FOCK_OK;
+  const int64_t blocks = (total * 32 + 255) / 256;
+  FOCK_CUDA_TRY(launch_kernel(reduce_ops_kernel, dim3((unsigned)blocks, nb), dim3(256), 0, st, 0, ops, n_ops, total, D,
+                               cpart, carena, part_stride, out_stride));
+  return FOCK_OK;
+}

@@ -158,6 +158,17 @@ int launch_adjoint_partials(int dtype, const void* psi_in, const void* lam_out, 
                             double2* cpart, const AdjSched& sc, cudaStream_t st, const BatchArg& bt = BatchArg());
 int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* cout, cudaStream_t st, int nb = 1,
                            int64_t part_stride = 0, int64_t out_stride = 0, int pdl = 0);
+// All ops' partials in one launch: op k's partials sit at cpart_off; entry e
+// of its C (stored orientation) is the fixed-order sum over x < gx of
+// cpart[cpart_off + x * nent + e] (plane layout) or of
+// cpart[cpart_off + gx * blk_offset(bs) + x * s^2 + e_in_block] (block
+// schedules, one gx for every block).
+struct RedOp {
+  int64_t c_off, cpart_off;
+  int nent, gx, plane, layout;
+};
+int launch_reduce_ops(const RedOp* ops, int n_ops, int64_t total, int D, const double2* cpart, double2* carena,
+                      cudaStream_t st, int nb, int64_t part_stride, int64_t out_stride);
 // sum the partials of a schedule into `cout` (stored orientation, layout entries)
 int launch_reduce_sched(const double2* cpart, const AdjSched& sc, int D, int layout, double2* cout, cudaStream_t st,
                         int nb = 1, int64_t part_stride = 0, int64_t out_stride = 0, int pdl = 0);

@@ -49,6 +49,7 @@ struct PlanOp {
   // persistent-sweep adjoint schedule and partial-sum region
   AdjSched psched;
   int64_t ppart_off = 0;
+  int64_t cpart_off = 0;  // this op's partial-sum region (reduce_at_end)
 };
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -71,6 +72,10 @@ struct fock_plan {
   // workspace sections
   size_t o_arena = 0, o_carena = 0, o_cpart = 0, ws_bytes = 0;
   int64_t arena_entries = 0, carena_entries = 0, cpart_entries = 0;
+  // partial sums: one region per op, reduced by one launch after the sweep
+  // (when they fit the budget), or one shared region reduced after every op
+  int reduce_at_end = 0;
+  size_t o_red = 0;
   int64_t state_elems = 0;
   int64_t flops_fwd = 0;
   // persistent sweeps (small states): grids, tables, sync words, partials
@@ -380,7 +385,7 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
     P->persist = P->g_fwd > 0 && P->g_bwd > 0;
   }
   int64_t ppart = 0;
-  int64_t arena = 0, carena = 0, cpart = 0;
+  int64_t arena = 0, carena = 0, cpart = 0, cpart_sum = 0;
   int n_terms = 0, n_contrib = 0;
   for (size_t k = 0; k < P->ops.size(); ++k) {
     PlanOp& op = P->ops[k];
@@ -418,9 +423,10 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
     }
     op.c_off = carena;
     carena += op.nent;
-    // one partial-sum region shared by all ops: each op's partials are
-    // reduced right after its adjoint launch
-    cpart = std::max<int64_t>(cpart, op.plane ? (int64_t)op.grid_adj * op.pg_adj.nent : op.sched.part_entries);
+    const int64_t part_k = op.plane ? (int64_t)op.grid_adj * op.pg_adj.nent : op.sched.part_entries;
+    op.cpart_off = cpart_sum;
+    cpart_sum += part_k;
+    cpart = std::max<int64_t>(cpart, part_k);
     n_terms += (int)op.terms.size();
     n_contrib += (int)op.contribs.size();
     // flops: 8 real flops per complex multiply-add
@@ -429,7 +435,10 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   }
   P->arena_entries = arena;
   P->carena_entries = carena;
-  P->cpart_entries = cpart;
+  // every op's partials kept until one reduction after the sweep when that
+  // costs at most 512 MiB (about 280 MB for the 6-mode cutoff-12 CV-QNN)
+  P->reduce_at_end = (double)cpart_sum * batch * sizeof(double2) <= 512.0 * (1 << 20);
+  P->cpart_entries = P->reduce_at_end ? cpart_sum : cpart;
   P->n_terms = n_terms;
   P->n_contrib = n_contrib;
   const int n_ops = (int)P->ops.size();
@@ -443,10 +452,11 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   P->o_pstart = o; o = align256(o + sizeof(int) * (n_params + 1));
   P->o_plist = o; o = align256(o + sizeof(int) * std::max(n_contrib, 1));
   if (P->persist) { P->o_sweep = o; o = align256(o + sizeof(SweepOp) * std::max(n_ops, 1)); }
+  P->o_red = o; o = align256(o + sizeof(RedOp) * std::max(n_ops, 1));
   P->tables_bytes = o;
   P->o_arena = o; o = align256(o + sizeof(double2) * arena * batch);
   P->o_carena = o; o = align256(o + sizeof(double2) * std::max<int64_t>(carena, 1) * batch);
-  P->o_cpart = o; o = align256(o + sizeof(double2) * std::max<int64_t>(cpart, 1) * batch);
+  P->o_cpart = o; o = align256(o + sizeof(double2) * std::max<int64_t>(P->cpart_entries, 1) * batch);
   if (P->persist) {
     P->ppart_entries = ppart;
     P->o_sync = o; o = align256(o + (4 + n_ops) * sizeof(unsigned));
@@ -499,6 +509,16 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
       by_param[gc.pidx].push_back(c);
       ++c;
     }
+  }
+  RedOp* red = (RedOp*)(P->host + P->o_red);
+  for (int k = 0; k < n_ops; ++k) {
+    const PlanOp& op = P->ops[k];
+    red[k].c_off = op.c_off;
+    red[k].cpart_off = op.cpart_off;
+    red[k].nent = (int)op.nent;
+    red[k].gx = op.plane ? op.grid_adj : op.sched.gx[0];
+    red[k].plane = op.plane;
+    red[k].layout = op.layout;
   }
   if (P->persist) {
     SweepOp* sw_ops = (SweepOp*)(P->host + P->o_sweep);
@@ -689,18 +709,21 @@ static int adjoint_op(BwdCtx& b, int k, const void* psi_in) {
   int rc;
   if (P->timing && (rc = record_event(P->ev_bwd[k + 1], st))) return rc;
   double2* cout = (double2*)(b.ws + P->o_carena) + op.c_off;
+  double2* part = b.cpart + (P->reduce_at_end ? op.cpart_off : 0);
   if (op.plane) {
     rc = launch_plane_adjoint(P->dtype, psi_in, b.lam, b.other, op.pg_adj, op.grid_adj, b.c.arena + op.m_off,
-                              op_flags(op), b.cpart, st, b.c.bt);
+                              op_flags(op), part, st, b.c.bt);
     if (rc) return rc;
-    rc = launch_reduce_partials(b.cpart, op.grid_adj, op.nent, cout, st, P->batch, P->cpart_entries,
-                                P->carena_entries, b.pdl);
+    if (!P->reduce_at_end)
+      rc = launch_reduce_partials(part, op.grid_adj, op.nent, cout, st, P->batch, P->cpart_entries,
+                                  P->carena_entries, b.pdl);
   } else {
     rc = launch_adjoint_partials(P->dtype, psi_in, b.lam, b.other, op.view, P->D, op.layout, b.c.arena + op.m_off,
-                                 op_flags(op), b.cpart, op.sched, st, b.c.bt);
+                                 op_flags(op), part, op.sched, st, b.c.bt);
     if (rc) return rc;
-    rc = launch_reduce_sched(b.cpart, op.sched, P->D, op.layout, cout, st, P->batch, P->cpart_entries,
-                             P->carena_entries, b.pdl);
+    if (!P->reduce_at_end)
+      rc = launch_reduce_sched(part, op.sched, P->D, op.layout, cout, st, P->batch, P->cpart_entries,
+                               P->carena_entries, b.pdl);
   }
   if (rc) return rc;
   b.c.bt.pdl = b.pdl;
@@ -849,6 +872,11 @@ extern "C" int fock_plan_backward_recompute(fock_plan* P, const double* params, 
   if (P->timing) {
     if ((rc = record_event(P->ev_bwd[0], st))) return rc;
     P->bwd_recorded = 1;
+  }
+  if (P->reduce_at_end && n_ops > 0) {
+    rc = launch_reduce_ops((const RedOp*)(ws + P->o_red), n_ops, P->carena_entries, P->D, b.cpart,
+                           (double2*)(ws + P->o_carena), st, P->batch, P->cpart_entries, P->carena_entries);
+    if (rc) return rc;
   }
   if (lam != grad_state) FOCK_CUDA_TRY(cudaMemcpyAsync(grad_state, lam, c.sb, cudaMemcpyDeviceToDevice, st));
   return param_grads(P, ws, c, grad_params, st);
