@@ -85,8 +85,9 @@ struct ApplyDispatch<CT, DMAX + 1, DMAX, COH> {
   }
 };
 
-// 4 resident CTAs (32 warps) per SM for cutoffs up to 12, 2 beyond
-template <int DMAX> struct ApplyMinBlocks { static const int value = (DMAX > 0 && DMAX <= 12) ? 4 : 2; };
+// resident CTAs per SM the register budget allows: 4 (32 warps) up to cutoff
+// 12, 3 up to 20 (the batched workload's bulk), 2 beyond
+template <int DMAX> struct ApplyMinBlocks { static const int value = (DMAX > 0 && DMAX <= 12) ? 4 : (DMAX > 0 && DMAX <= 20) ? 3 : 2; };
 
 
 template <int S> struct RRof { static const int value = (S + 3) / 4; };
@@ -263,8 +264,10 @@ struct AdjDispatch<CT, DMAX + 1, DMAX, TILE> {
   }
 };
 
-// 3 resident CTAs (24 warps) per SM for complex64 cutoffs up to 12
+// register budget of the adjoint: 3 resident CTAs (24 warps) per SM for
+// complex64 cutoffs up to 12, 2 up to 20 (a few hundred bytes of spill at 20,
+// measured 18% faster on the heterogeneous batch than 1 CTA/SM), else 1
 template <typename CT, int DMAX> struct AdjMinBlocks {
-  static const int value = (sizeof(CT) == 8 && DMAX > 0 && DMAX <= 12) ? 3 : 1;
+  static const int value = (sizeof(CT) == 8 && DMAX > 0 && DMAX <= 12) ? 3 : (sizeof(CT) == 8 && DMAX > 0 && DMAX <= 20) ? 2 : 1;
 };
 
