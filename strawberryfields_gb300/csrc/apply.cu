@@ -16,6 +16,12 @@
 // FMAs are fully unrolled.
 #include "apply.cuh"
 
+static void set_fastdiv(AxisView& v) {
+  v.fast = v.ncols < ((int64_t)1 << 32);
+  v.fc = make_fastdiv(v.fast ? (uint32_t)v.C : 1u);
+  v.fb = make_fastdiv(v.fast ? (uint32_t)v.B : 1u);
+}
+
 AxisView make_view1(int naxes, int D, int ax) {
   AxisView v;
   int64_t C = 1;
@@ -24,6 +30,7 @@ AxisView make_view1(int naxes, int D, int ax) {
   for (int k = 0; k < ax; ++k) A *= D;
   v.A = A; v.B = 1; v.C = C; v.s1 = C; v.s2 = 0;
   v.ncols = A * C;
+  set_fastdiv(v);
   return v;
 }
 
@@ -37,6 +44,7 @@ AxisView make_view2(int naxes, int D, int ax1, int ax2) {
   v.s2 = C;
   v.s1 = B * D * C;
   v.ncols = A * B * C;
+  set_fastdiv(v);
   return v;
 }
 

@@ -3,6 +3,28 @@
 #pragma once
 #include "gates.cuh"
 
+// Exact division of a 32-bit numerator by a runtime constant d >= 1 as a
+// multiply-high and two shifts (round-up multiplier with the add correction:
+// m = floor(2^32 (2^l - d) / d) + 1, l = ceil(log2 d);
+// q = (t + ((n - t) >> 1)) >> (l - 1) with t = (n * m) >> 32).
+struct FastDiv {
+  uint32_t d, m;
+  int l;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f;
+  f.d = d;
+  f.l = 0;
+  while ((1ull << f.l) < d) ++f.l;
+  f.m = d == 1 ? 0u : (uint32_t)((((uint64_t)1 << 32) * ((1ull << f.l) - d)) / d + 1);
+  return f;
+}
+__host__ __device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+  if (f.d == 1) return n;
+  const uint32_t t = (uint32_t)(((uint64_t)n * f.m) >> 32);
+  return (t + ((n - t) >> 1)) >> (f.l - 1);
+}
+
 // A gate on axes (ax1 < ax2) of a C-order [D]^naxes tensor sees the state as
 // [A][D][B][D][C] (two axes) or [A][D][C] (one axis; B = 1, s2 = 0).
 // Column j = (a, b, c), c fastest; element (a, i, b, k, c) sits at
@@ -11,12 +33,22 @@ struct AxisView {
   int64_t A, B, C;
   int64_t s1, s2;
   int64_t ncols;
+  int fast;         // ncols < 2^32: column indices decomposed by FastDiv
+  FastDiv fc, fb;   // division by C and by B
 };
 
 AxisView make_view1(int naxes, int D, int ax);
 AxisView make_view2(int naxes, int D, int ax1, int ax2);
 
 __device__ __forceinline__ int64_t col_base(const AxisView& v, int64_t j, int D) {
+  if (v.fast) {
+    const uint32_t jj = (uint32_t)j;
+    const uint32_t t = fdiv(jj, v.fc);
+    const uint32_t c = jj - t * (uint32_t)v.C;
+    const uint32_t a = fdiv(t, v.fb);
+    const uint32_t b = t - a * (uint32_t)v.B;
+    return (int64_t)a * (v.s1 * D) + (int64_t)b * (v.s2 * D) + c;
+  }
   int64_t c = j % v.C;
   int64_t t = j / v.C;
   int64_t b = t % v.B;
