@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)
   const int bs = layout == LAYOUT_DENSE ? 0 : ((layout == LAYOUT_DIFF && (mflags & MF_SWAP)) ? 2 * D - 2 - b : b);
   double2* mypart = cpart + sc.part_off[bs] + (int64_t)xrank * s * s;
   CT* MsH = reinterpret_cast<CT*>(smem_raw);
-  CT* lam_s = MsH + ((s * s + 1) & ~1);
+  CT* lam_s = MsH + ((s * ms_stride<CT>(s) + 1) & ~1);
   CT* psi_s = lam_s + rows * (TILE + 1);
   pdl_wait();
   pdl_launch_dependents();
@@ -63,7 +63,7 @@ static size_t adjoint_smem(int dtype, int D) {
   const int esz = dtype == FOCK_C64 ? 8 : 16;
   const int rows = 4 * ((D + 3) / 4);
   // matrix + the lam and psi tiles
-  return (size_t)esz * ((size_t)((D * D + 1) & ~1) + 2 * (size_t)rows * (tile_of(dtype) + 1));
+  return (size_t)esz * ((size_t)((D * (D + 1) + 1) & ~1) + 2 * (size_t)rows * (tile_of(dtype) + 1));
 }
 
 template <typename CT, int TILE, int DMAX>

@@ -106,11 +106,19 @@ __device__ __forceinline__ BlockGeom block_geom(const AxisView& v, int D, int la
   return g;
 }
 
+// Row stride of a staged s x s block: complex64 rows are padded to an even
+// length, so one 16-byte shared load carries two entries (row_mac).
+template <typename CT>
+__host__ __device__ __forceinline__ int ms_stride(int s) {
+  return sizeof(CT) == 8 ? (s + 1) & ~1 : s;
+}
+
 // Stage the s x s block for this CTA into shared memory in the state precision,
-// as the matrix that maps the view's input positions to its output positions.
+// as the matrix that maps the view's input positions to its output positions
+// (row w at Ms + w * ms_stride(s)).
 template <typename CT>
 __device__ __forceinline__ void stage_block(CT* Ms, const double2* mat, const BlockGeom& g, int mflags) {
-  const int s = g.s;
+  const int s = g.s, sp = ms_stride<CT>(s);
   for (int e = threadIdx.x; e < s * s; e += blockDim.x) {
     int w = e / s, u = e - w * s;  // view output w, view input u
     int a = w, c = u;
@@ -119,8 +127,26 @@ __device__ __forceinline__ void stage_block(CT* Ms, const double2* mat, const Bl
     double2 m = mat[g.moff + (int64_t)a * s + c];
     int cj = ((mflags & MF_ADJOINT) ? 1 : 0) ^ ((mflags & MF_CONJ) ? 1 : 0);
     if (cj) m.y = -m.y;
-    Ms[e] = to_c(m, (CT*)nullptr);
+    Ms[w * sp + u] = to_c(m, (CT*)nullptr);
   }
+}
+
+// a += sum_u row[u] x[u] over one staged row (16-byte loads of entry pairs
+// for complex64; rows start on 16-byte boundaries)
+template <int S>
+__device__ __forceinline__ void row_mac(float2& a, const float2* row, const float2 (&x)[S]) {
+  const float4* r4 = reinterpret_cast<const float4*>(row);
+#pragma unroll
+  for (int u2 = 0; u2 < (S + 1) / 2; ++u2) {
+    const float4 m = r4[u2];
+    cfma(a, make_float2(m.x, m.y), x[2 * u2]);
+    if (2 * u2 + 1 < S) cfma(a, make_float2(m.z, m.w), x[2 * u2 + 1]);
+  }
+}
+template <int S>
+__device__ __forceinline__ void row_mac(double2& a, const double2* row, const double2 (&x)[S]) {
+#pragma unroll
+  for (int u = 0; u < S; ++u) cfma(a, row[u], x[u]);
 }
 
 // A batch of nb independent circuits of one structure: grid.z indexes the

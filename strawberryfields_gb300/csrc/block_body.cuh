@@ -40,11 +40,11 @@ __device__ __forceinline__ void apply_cols(const CT* __restrict__ in, CT* __rest
   stage_block(Ms, mat, g, mflags);
   __syncthreads();
   if (!valid) return;
+  constexpr int SP = sizeof(CT) == 8 ? (S + 1) & ~1 : S;
 #pragma unroll
   for (int w = 0; w < S; ++w) {
     CT a0 = czero<CT>();
-#pragma unroll
-    for (int u = 0; u < S; ++u) cfma(a0, Ms[w * S + u], x0[u]);
+    row_mac<S>(a0, Ms + w * SP, x0);
     out[b0 + w * g.step] = a0;
   }
 }
@@ -59,10 +59,10 @@ __device__ void apply_cols_generic(const CT* __restrict__ in, CT* __restrict__ o
     const int64_t j = j0 + k * APPLY_THREADS;
     if (j >= v.ncols) break;
     const int64_t base = col_base(v, j, D) + g.boff;
-    const int S = g.s;
+    const int S = g.s, SP = ms_stride<CT>(S);
     for (int w = 0; w < S; ++w) {
       CT acc = czero<CT>();
-      for (int u = 0; u < S; ++u) cfma(acc, Ms[w * S + u], ld_state<COH>(in + base + u * g.step));
+      for (int u = 0; u < S; ++u) cfma(acc, Ms[w * SP + u], ld_state<COH>(in + base + u * g.step));
       out[base + w * g.step] = acc;
     }
   }
@@ -124,10 +124,12 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
     for (int c = 0; c < RR; ++c) acc[r][c] = czero<CT>();
 
   const int64_t ntiles = (v.ncols + TILE - 1) / TILE;
+  int64_t tile_base = 0;  // this thread's column base in the last issued tile
   auto issue = [&](int64_t t) {
     const int64_t j = t * TILE + tid;
     const bool valid = j < v.ncols;
     const int64_t base = valid ? col_base(v, j, D) + g.boff : 0;
+    tile_base = base;
 #pragma unroll
     for (int u = 0; u < S; ++u) {
       const int64_t off = valid ? base + u * g.step : 0;
@@ -150,15 +152,15 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
     const int64_t j = t * TILE + tid;
     if (write_lam && j < v.ncols) {
       // each thread reads back only its own column: no barrier needed here
-      const int64_t base = col_base(v, j, D) + g.boff;
+      const int64_t base = tile_base;
+      constexpr int SP = sizeof(CT) == 8 ? (S + 1) & ~1 : S;
       CT lam[S];
 #pragma unroll
       for (int u = 0; u < S; ++u) lam[u] = lam_s[u * LD + tid];
 #pragma unroll
       for (int w = 0; w < S; ++w) {
         CT a = czero<CT>();
-#pragma unroll
-        for (int u = 0; u < S; ++u) cfma(a, MsH[w * S + u], lam[u]);
+        row_mac<S>(a, MsH + w * SP, lam);
         lam_in[base + w * g.step] = a;
       }
     }
@@ -232,9 +234,10 @@ __device__ void adjoint_generic(const CT* __restrict__ psi_in, const CT* __restr
   if (!write_lam) return;
   for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
     const int64_t base = col_base(v, j, D) + g.boff;
+    const int SP = ms_stride<CT>(S);
     for (int w = 0; w < S; ++w) {
       CT a = czero<CT>();
-      for (int u = 0; u < S; ++u) cfma(a, MsH[w * S + u], lam_out[base + u * g.step]);
+      for (int u = 0; u < S; ++u) cfma(a, MsH[w * SP + u], lam_out[base + u * g.step]);
       lam_in[base + w * g.step] = a;
     }
   }

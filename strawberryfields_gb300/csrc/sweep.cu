@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)
           layout == LAYOUT_DENSE ? 0 : ((layout == LAYOUT_DIFF && (mflags & MF_SWAP)) ? 2 * D - 2 - b : b);
       double2* mypart = cpart + op->part_base + sc.part_off[bs] + (int64_t)xrank * s * s;
       CT* MsH = reinterpret_cast<CT*>(smem_raw);
-      CT* lam_s = MsH + ((s * s + 1) & ~1);
+      CT* lam_s = MsH + ((s * ms_stride<CT>(s) + 1) & ~1);
       CT* psi_s = lam_s + rows * (TILE + 1);
       AdjDispatch<CT, 1, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, arena + op->m_off, mflags, lam_s,
                                           psi_s, g, mypart, xrank, gxb, 1);
@@ -182,12 +182,12 @@ __global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)
 // ---------------------------------------------------------------------------
 static int adj_tile(int dtype) { return dtype == FOCK_C64 ? 256 : 128; }
 
-static size_t fwd_smem(int dtype, int D) { return (size_t)D * D * (dtype == FOCK_C64 ? 8 : 16); }
+static size_t fwd_smem(int dtype, int D) { return (size_t)D * (D + 1) * (dtype == FOCK_C64 ? 8 : 16); }
 
 static size_t bwd_smem(int dtype, int D) {
   const int esz = dtype == FOCK_C64 ? 8 : 16;
   const int rows = 4 * ((D + 3) / 4);
-  return (size_t)esz * ((size_t)((D * D + 1) & ~1) + 2 * (size_t)rows * (adj_tile(dtype) + 1));
+  return (size_t)esz * ((size_t)((D * (D + 1) + 1) & ~1) + 2 * (size_t)rows * (adj_tile(dtype) + 1));
 }
 
 template <typename K>
