@@ -212,10 +212,13 @@ int fock_plan_backward(fock_plan* plan, const double* params, const void* state_
  * scratch slots, every chunk processed the same way, last chunk first -- so
  * the adjoint of a long segment (a density matrix of many GB between
  * checkpoints) runs in bounded memory at the cost of extra forward passes. */
+#define FOCK_BACKWARD_REUSE_BUILD 1 /* flags: `workspace` holds the matrices (and derivatives)
+                                     built by the last forward sweep with these `params`; skip the
+                                     rebuild */
 int fock_plan_backward_recompute(fock_plan* plan, const double* params, const void* state_in,
                                  const void* states, int store_every, void* seg, int seg_slots,
-                                 void* grad_state, void* grad_tmp, double* grad_params, void* workspace,
-                                 void* stream);
+                                 void* grad_state, void* grad_tmp, double* grad_params, int flags,
+                                 void* workspace, void* stream);
 
 /* Per-op device timing of plan sweeps (CUDA events recorded between the op
  * launches on the sweep's stream).  After enabling, every forward/backward

@@ -30,6 +30,7 @@ TWO_MODE_SQUEEZE = 6
 MZGATE = 7
 CROSS_KERR = 8
 LOSS = 9
+FOCK_BACKWARD_REUSE_BUILD = 1
 
 TWO_MODE_KINDS = (BEAMSPLITTER, TWO_MODE_SQUEEZE, MZGATE, CROSS_KERR)
 NPARAMS = {ROTATION: 1, KERR: 1, DISPLACEMENT: 2, SQUEEZE: 2, BEAMSPLITTER: 2, TWO_MODE_SQUEEZE: 2,
@@ -81,7 +82,7 @@ _SIGS = {
     "fock_plan_op": (_i, [_vp, _i, _ip, _ip, _ip, _ip]),
     "fock_plan_forward": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp]),
     "fock_plan_backward": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
-    "fock_plan_backward_recompute": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _vp]),
+    "fock_plan_backward_recompute": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _i, _vp, _vp, _vp, _i, _vp, _vp]),
     "fock_plan_enable_timing": (_i, [_vp, _i]),
     "fock_plan_op_times": (_i, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "fock_plan_sweep_status": (_i, [_vp, _vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),

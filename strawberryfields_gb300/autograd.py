@@ -83,6 +83,10 @@ class CompiledCircuit:
         self.shape = [self.cutoff] * (self.num_modes if self.pure else 2 * self.num_modes)
         self._bshape = ([self.batch] if self.batch > 1 else []) + self.shape
         self._ws_buf = None
+        # the workspace's matrices were built by forward sweep number _fwd_n
+        # for the parameter buffer (data pointer, version) _built_for
+        self._fwd_n = 0
+        self._built_for = None
         self._vacuum = torch.zeros([self.batch, int(info.state_elems)], dtype=self.dtype, device=self.device)
         self._vacuum[:, 0] = 1.0
         self._vacuum = self._vacuum.reshape(self._bshape)
@@ -106,6 +110,7 @@ class CompiledCircuit:
     def release(self):
         """Drop the workspace until the next sweep (memory reuse across plans)."""
         self._ws_buf = None
+        self._built_for = None
 
     @property
     def n_ops(self):
@@ -165,6 +170,8 @@ class CompiledCircuit:
         L.check(L.load().fock_plan_forward(self._plan, p.data_ptr(), x.data_ptr(), states.data_ptr(),
                                            k, self._ws.data_ptr(), self._stream()),
                 "fock_plan_forward")
+        self._fwd_n += 1
+        self._built_for = (p.data_ptr(), p._version, self._fwd_n)
         if not store_all:
             return states[self.final_index(0)]
         return states
@@ -189,9 +196,13 @@ class CompiledCircuit:
         k = self.checkpoint
         nslot = self.recompute_slots
         seg = torch.empty([nslot] + self._bshape, dtype=self.dtype, device=self.device) if k > 1 else None
+        # the last forward sweep on this workspace built the matrices for the
+        # same parameter buffer, unmodified since: skip the rebuild
+        reuse = self._ws_buf is not None and self._built_for == (p.data_ptr(), p._version, self._fwd_n)
+        flags = L.FOCK_BACKWARD_REUSE_BUILD if reuse else 0
         L.check(L.load().fock_plan_backward_recompute(self._plan, p.data_ptr(), x.data_ptr(), states.data_ptr(), k,
                                                       seg.data_ptr() if seg is not None else None, nslot,
-                                                      lam.data_ptr(), tmp.data_ptr(), grads.data_ptr(),
+                                                      lam.data_ptr(), tmp.data_ptr(), grads.data_ptr(), flags,
                                                       self._ws.data_ptr(), self._stream()),
                 "fock_plan_backward_recompute")
         return grads, lam

@@ -109,6 +109,7 @@ AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout) {
   AdjSched sc;
   memset(&sc, 0, sizeof(sc));
   sc.nblk = layout == LAYOUT_DENSE ? 1 : 2 * D - 1;
+  if (sc.nblk > ADJ_MAX_BLOCKS) sc.nblk = 0;  // cutoff beyond FOCK_MAX_CUTOFF: callers reject it first
   const int64_t ntiles = (v.ncols + tile_of(dtype) - 1) / tile_of(dtype);
   // the same number of CTAs for every block (small blocks are memory-bound
   // and need as many as large ones), about 8 CTAs per SM in total; largest

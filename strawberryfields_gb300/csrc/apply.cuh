@@ -195,13 +195,12 @@ int launch_apply(int dtype, const void* in, void* out, const AxisView& v, int D,
 // Adjoint step of one op: lam_in = M^dagger lam_out (skipped when lam_in is
 // null) and the per-CTA partial sums of
 // C[u][v] = sum over columns conj(lam_out[u]) psi_in[v] (stored-matrix
-// orientation, FP64), written to cpart[gx][entries] with gx =
-// adjoint_grid_x(...).  launch_reduce_partials sums them in a fixed order.
-// CTA schedule of one adjoint launch: block b (view orientation) gets gx[b]
-// persistent CTAs, in proportion to its s_b^2 work; CTAs start[b] ..
-// start[b+1]-1 serve it.  Partial sums of stored-orientation block bs sit at
-// part_off[bs] + x * s^2 (x < gx of that size).
-#define ADJ_MAX_BLOCKS 48
+// orientation, FP64).  CTA schedule of one launch: view block y gets gx[y]
+// CTAs (the same number for every block), CTAs start[y] .. start[y+1]-1;
+// the partial sums of stored block bs sit at part_off[bs] + x * s^2 (x < gx),
+// summed in a fixed order by launch_reduce_sched or launch_reduce_ops.
+// one entry per photon-number block: 2D - 1 blocks at the largest cutoff
+#define ADJ_MAX_BLOCKS (2 * FOCK_MAX_CUTOFF - 1)
 struct AdjSched {
   int nblk;
   int total;

@@ -804,13 +804,13 @@ extern "C" int fock_plan_backward(fock_plan* P, const double* params, const void
                                   const void* states, int store_every, void* seg, void* grad_state,
                                   void* grad_tmp, double* grad_params, void* workspace, void* stream) {
   return fock_plan_backward_recompute(P, params, state_in, states, store_every, seg,
-                                      store_every > 1 ? store_every - 1 : 0, grad_state, grad_tmp, grad_params,
+                                      store_every > 1 ? store_every - 1 : 0, grad_state, grad_tmp, grad_params, 0,
                                       workspace, stream);
 }
 
 extern "C" int fock_plan_backward_recompute(fock_plan* P, const double* params, const void* state_in,
                                             const void* states, int store_every, void* seg, int seg_slots,
-                                            void* grad_state, void* grad_tmp, double* grad_params,
+                                            void* grad_state, void* grad_tmp, double* grad_params, int flags,
                                             void* workspace, void* stream) {
   if (!P) return fock_set_error(FOCK_ERR_INVALID, "null plan");
   if (!state_in || !states || !grad_state || !grad_tmp || !workspace)
@@ -821,8 +821,10 @@ extern "C" int fock_plan_backward_recompute(fock_plan* P, const double* params, 
   if (P->n_params > 0 && (!params || !grad_params)) return fock_set_error(FOCK_ERR_INVALID, "null parameter array");
   cudaStream_t st = (cudaStream_t)stream;
   unsigned char* ws = (unsigned char*)workspace;
-  int rc = upload_and_build(P, params, ws, 1, st);
-  if (rc) return rc;
+  int rc = 0;
+  // the forward sweep builds M and dM: reuse them when the caller says the
+  // workspace still holds that sweep's build for these parameters
+  if (!(flags & FOCK_BACKWARD_REUSE_BUILD) && (rc = upload_and_build(P, params, ws, 1, st))) return rc;
   SweepCtx c;
   sweep_ctx(P, ws, st, &c);
   const int n_ops = (int)P->ops.size();

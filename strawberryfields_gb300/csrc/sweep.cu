@@ -239,6 +239,7 @@ AdjSched make_adj_sched_grid(int dtype, const AxisView& v, int D, int layout, in
   AdjSched sc;
   memset(&sc, 0, sizeof(sc));
   sc.nblk = layout == LAYOUT_DENSE ? 1 : 2 * D - 1;
+  if (sc.nblk > ADJ_MAX_BLOCKS) sc.nblk = 0;  // cutoff beyond FOCK_MAX_CUTOFF: callers reject it first
   const int64_t ntiles = (v.ncols + adj_tile(dtype) - 1) / adj_tile(dtype);
   // the same number of CTAs for every block, all of them within the grid
   int64_t gx = grid / sc.nblk;

@@ -214,3 +214,64 @@ def test_checkpointed_adjoint_matches_stored(cuda, k):
         out.append((psi.detach().cpu().numpy(), p.grad.cpu().numpy()))
     assert np.abs(out[0][0] - out[1][0]).max() < 1e-13
     assert np.abs(out[0][1] - out[1][1]).max() < 1e-12
+
+
+@pytest.mark.parametrize("D", [3, 7, 11, 14, 19, 23, 26])
+def test_gradient_every_cutoff_bucket(cuda, D):
+    """Forward and adjoint parity in every compiled cutoff bucket (4, 8, 12,
+    16, 20, 24) and on the generic path beyond 24, complex128 and complex64:
+    dense single-mode ops, beamsplitters on an inner pair and on the last
+    pair (plane kernels up to cutoff 16), a swapped two-mode squeezer."""
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+
+    N = 3
+    gates = [(4, 0, -1, 0), (3, 2, -1, 2), (5, 0, 1, 4), (5, 1, 2, 6), (6, 2, 0, 8), (1, 1, -1, 10),
+             (3, 1, -1, 11), (5, 2, 1, 13)]
+    npar = 15
+    rng = np.random.default_rng(D)
+    params = rng.uniform(0.05, 0.35, npar)
+    t = rng.normal(size=(D,) * N) + 1j * rng.normal(size=(D,) * N)
+    t /= np.linalg.norm(t)
+    ref_states = fo.run_gates(gates, params, N, D)
+    _, g_final = _loss_grad(ref_states[-1], t)
+    ref = fo.adjoint_grads(gates, params, N, D, g_final)
+    for tdt, tol_s, tol_g in ((torch.complex128, 1e-11, 1e-9), (torch.complex64, 1e-5, 1e-4)):
+        circ = CompiledCircuit(N, D, gates, npar, dtype=tdt)
+        p = torch.tensor(params, device="cuda", requires_grad=True)
+        psi = circ(p)
+        assert np.abs(psi.detach().to(torch.complex128).cpu().numpy() - ref_states[-1]).max() < tol_s
+        tt = torch.as_tensor(t, device="cuda").to(tdt)
+        loss = 1 - torch.abs(torch.sum(tt.conj() * psi)) ** 2
+        loss.backward()
+        got = p.grad.cpu().numpy()
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < tol_g, (D, tdt)
+
+
+def test_backward_reuses_or_rebuilds_matrices(cuda):
+    """The adjoint sweep reuses the forward sweep's matrices only when the
+    workspace still holds them for the same, unmodified parameters."""
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+    from strawberryfields_gb300.qnn import qnn_gates, qnn_params
+
+    gates, npar = qnn_gates(3, 2)
+    p1 = torch.tensor(qnn_params(gates, npar, seed=1), device="cuda")
+    p2 = torch.tensor(qnn_params(gates, npar, seed=2), device="cuda")
+    g_state = torch.randn(6, 6, 6, dtype=torch.complex128, device="cuda")
+
+    def fresh(p):
+        c = CompiledCircuit(3, 6, gates, npar, dtype=torch.complex128)
+        s = c.forward_states(p)
+        return c.backward(p, s, g_state)[0]
+
+    ref1, ref2 = fresh(p1), fresh(p2)
+    c = CompiledCircuit(3, 6, gates, npar, dtype=torch.complex128)
+    s1 = c.forward_states(p1)
+    s2 = c.forward_states(p2)  # the workspace now holds p2's matrices
+    assert torch.allclose(c.backward(p1, s1, g_state)[0], ref1, rtol=1e-12, atol=1e-14)
+    s2 = c.forward_states(p2)
+    assert torch.allclose(c.backward(p2, s2, g_state)[0], ref2, rtol=1e-12, atol=1e-14)  # reused
+    s1 = c.forward_states(p1)
+    p1.mul_(1.0)  # in-place update: version changes, matrices rebuilt
+    assert torch.allclose(c.backward(p1, s1, g_state)[0], ref1, rtol=1e-12, atol=1e-14)
