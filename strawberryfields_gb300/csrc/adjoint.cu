@@ -25,6 +25,8 @@
 
 #include <string.h>
 
+#include <algorithm>
+
 template <typename CT, int TILE, int DMAX>
 __global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)
     adjoint_block_kernel(const CT* __restrict__ psi_in, const CT* __restrict__ lam_out, CT* __restrict__ lam_in,
@@ -66,56 +68,17 @@ static size_t adjoint_smem(int dtype, int D) {
   return (size_t)esz * ((size_t)((D * (D + 1) + 1) & ~1) + 2 * (size_t)rows * (tile_of(dtype) + 1));
 }
 
-template <typename CT, int TILE, int DMAX>
-static int resident_ctas(size_t sm) {
-  auto k = adjoint_block_kernel<CT, TILE, DMAX>;
-  int per_sm = 0;
-  // without a usable device (host-only plan building) assume one CTA per SM
-  if ((sm > 48 * 1024 &&
-       cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, TILE, sm) != cudaSuccess || per_sm < 1) {
-    cudaGetLastError();
-    per_sm = 1;
-  }
-  return per_sm * fock_num_sms();
-}
-
-static int adj_resident(int dtype, int D) {
-  const size_t sm = adjoint_smem(dtype, D);
-  const int b = dmax_bucket(D);
-  if (dtype == FOCK_C64) {
-    switch (b) {
-      case 4: return resident_ctas<float2, 256, 4>(sm);
-      case 8: return resident_ctas<float2, 256, 8>(sm);
-      case 12: return resident_ctas<float2, 256, 12>(sm);
-      case 16: return resident_ctas<float2, 256, 16>(sm);
-      case 20: return resident_ctas<float2, 256, 20>(sm);
-      case 24: return resident_ctas<float2, 256, 24>(sm);
-      default: return resident_ctas<float2, 256, 0>(sm);
-    }
-  }
-  switch (b) {
-    case 4: return resident_ctas<double2, 128, 4>(sm);
-    case 8: return resident_ctas<double2, 128, 8>(sm);
-    case 12: return resident_ctas<double2, 128, 12>(sm);
-    case 16: return resident_ctas<double2, 128, 16>(sm);
-    case 20: return resident_ctas<double2, 128, 20>(sm);
-    case 24: return resident_ctas<double2, 128, 24>(sm);
-    default: return resident_ctas<double2, 128, 0>(sm);
-  }
-}
-
-AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout) {
+AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout, int nb) {
   AdjSched sc;
   memset(&sc, 0, sizeof(sc));
   sc.nblk = layout == LAYOUT_DENSE ? 1 : 2 * D - 1;
   if (sc.nblk > ADJ_MAX_BLOCKS) sc.nblk = 0;  // cutoff beyond FOCK_MAX_CUTOFF: callers reject it first
   const int64_t ntiles = (v.ncols + tile_of(dtype) - 1) / tile_of(dtype);
   // the same number of CTAs for every block (small blocks are memory-bound
-  // and need as many as large ones), about 8 CTAs per SM in total; largest
-  // blocks come first in the flat grid so they start first
-  const int target = 8 * fock_num_sms();
-  (void)adj_resident;
+  // and need as many as large ones), about 8 CTAs per SM over all nb
+  // circuits of a batch (grid.z); largest blocks come first in the flat grid
+  // so they start first
+  const int target = std::max(1, 8 * fock_num_sms() / std::max(nb, 1));
   int64_t part = 0;
   int start = 0;
   for (int y = 0; y < sc.nblk; ++y) {

@@ -209,7 +209,8 @@ struct AdjSched {
   int start[ADJ_MAX_BLOCKS + 1];
   int64_t part_off[ADJ_MAX_BLOCKS];
 };
-AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout);
+// nb: circuits of a batch launched together (grid.z)
+AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout, int nb = 1);
 int launch_adjoint_partials(int dtype, const void* psi_in, const void* lam_out, void* lam_in,
                             const AxisView& v, int D, int layout, const double2* mat, int mflags,
                             double2* cpart, const AdjSched& sc, cudaStream_t st, const BatchArg& bt = BatchArg());

@@ -409,7 +409,7 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
       op.swap = a > b;
       op.view = make_view2(naxes, D, std::min(a, b), std::max(a, b));
     }
-    op.sched = make_adj_sched(dtype, op.view, D, op.layout);
+    op.sched = make_adj_sched(dtype, op.view, D, op.layout, batch);
     op.plane = use_plane && (force_plane || plane_preferred(op.layout, op.view)) && make_plane_geom(dtype, op.view, D, op.layout, op.swap, 0, &op.pg_fwd) &&
                make_plane_geom(dtype, op.view, D, op.layout, op.swap, 1, &op.pg_adj);
     if (op.plane) {
