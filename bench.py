@@ -206,6 +206,7 @@ def gpu_arm(args, rank, world, cpu_base):
     import torch
 
     from strawberryfields_gb300 import CompiledCircuit, _lib
+    from strawberryfields_gb300.qnn import qnn_params as qnn_params_fn
     from strawberryfields_gb300.qnn import target_state
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
@@ -332,6 +333,37 @@ def gpu_arm(args, rank, world, cpu_base):
     grad_err = float(torch.linalg.vector_norm(g64 - g128) / torch.linalg.vector_norm(g128))
     del circ128, psi
 
+    # throughput with a batch of parameter sets: B circuits of the same
+    # structure per plan (grid.z), one CUDA graph per step
+    batched = None
+    if not args.eager and args.batch > 1:
+        B = args.batch
+        circ_b = CompiledCircuit(N_MODES, CUTOFF, gates, npar, dtype=torch.complex64, device=dev, batch=B)
+        pb = torch.stack([torch.tensor(qnn_params_fn(gates, npar, seed=100 + i), device=dev) for i in range(B)])
+
+        def loss_b(psi):
+            s = torch.sum(t.conj() * psi, dim=tuple(range(1, psi.dim())))
+            return torch.sum(1 - (s.real ** 2 + s.imag ** 2))
+
+        gb = GraphedGradient(circ_b, loss_b, pb, warmup=1)
+        for _ in range(args.warmup):
+            gb(pb)
+        torch.cuda.synchronize()
+        eb0, eb1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        bt = []
+        for _ in range(args.steps):
+            flush.zero_()
+            eb0.record(st)
+            gb(pb)
+            eb1.record(st)
+            eb1.synchronize()
+            bt.append(eb0.elapsed_time(eb1))
+        ms_b = float(np.median(bt))
+        batched = {"circuits_per_step": B, "ms_per_step": ms_b, "grads_per_s": B * 1e3 / ms_b,
+                   "note": "B parameter sets of the same circuit in one batched plan (grid.z), gradient of the "
+                           "summed loss w.r.t. every set's parameters"}
+        del gb, circ_b
+
     # plain GPU forward + central differences
     for _ in range(3):
         circ.forward_states(p_dev, store_all=False)
@@ -387,6 +419,7 @@ def gpu_arm(args, rank, world, cpu_base):
         "grad_rel_err_vs_fp64": grad_err,
         "fd_baseline": {"gpu_forward_ms": 1e3 * fwd_s, "grads_per_s": fd_grads_per_s,
                         "adjoint_speedup": value / world / fd_grads_per_s},
+        "batched_throughput": batched,
         "clocks": clk, "cpu_baseline": cpu_base,
     }
     return out
@@ -621,6 +654,8 @@ def main():
     ap.add_argument("--only", default="", help="single-gate case: comma-separated subset of the kernels")
     ap.add_argument("--modes", type=int, default=7, help="single-gate case: modes of the cutoff-12 ket")
     ap.add_argument("--eager", action="store_true", help="no CUDA graph capture")
+    ap.add_argument("--batch", type=int, default=16,
+                    help="gradient case: parameter sets per step of the extra batched-throughput line")
     args = ap.parse_args()
     if args.case == "single-gate":
         return single_gate_case(args)
