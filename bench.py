@@ -200,6 +200,16 @@ def _traffic():
     return out
 
 
+def _autotune(circ, p):
+    cfgs, ms0, ms1 = circ.autotune(p)
+    ctas = {}
+    for fam, c in cfgs:
+        if fam == 0:
+            ctas[str(c)] = ctas.get(str(c), 0) + 1
+    return {"sweep_ms_before": round(ms0, 4), "sweep_ms_after": round(ms1, 4),
+            "plane_ops": sum(1 for fam, _ in cfgs if fam == 1), "block_ops_by_adjoint_ctas_per_sm": ctas}
+
+
 def gpu_arm(args, rank, world, cpu_base):
     import ctypes
 
@@ -228,6 +238,9 @@ def gpu_arm(args, rank, world, cpu_base):
     for _ in range(args.warmup):
         step(p_dev)
     torch.cuda.synchronize()
+    # per-op kernel family and adjoint CTA density picked by timing (before
+    # any capture: tuning reallocates the workspace)
+    tune = _autotune(circ, p_dev) if not args.no_autotune else None
     lib = _lib.load()
     # forward + loss + adjoint captured as one CUDA graph (no per-op events
     # inside the timed graph)
@@ -300,7 +313,10 @@ def gpu_arm(args, rank, world, cpu_base):
     peak, peak_kind = _peaks()
     groups = {}
     for k, (kind, m1, m2, nf) in enumerate(ops):
-        name = "dense1" if kind == 1 else "block2"
+        if circ.op_config(k)[0] == 1:
+            name = "plane1" if kind == 1 else "plane2"
+        else:
+            name = "dense1" if kind == 1 else "block2"
         for direction, arr, bytes_per in (("apply", fwd_ms, 2 * S), ("adjoint", bwd_ms, 3 * S)):
             key = f"{direction}_{name}"
             gsum = groups.setdefault(key, {"launches": 0, "ms": 0.0, "bytes": 0})
@@ -340,6 +356,7 @@ def gpu_arm(args, rank, world, cpu_base):
         B = args.batch
         circ_b = CompiledCircuit(N_MODES, CUTOFF, gates, npar, dtype=torch.complex64, device=dev, batch=B)
         pb = torch.stack([torch.tensor(qnn_params_fn(gates, npar, seed=100 + i), device=dev) for i in range(B)])
+        tune_b = _autotune(circ_b, pb) if not args.no_autotune else None
 
         def loss_b(psi):
             s = torch.sum(t.conj() * psi, dim=tuple(range(1, psi.dim())))
@@ -360,6 +377,7 @@ def gpu_arm(args, rank, world, cpu_base):
             bt.append(eb0.elapsed_time(eb1))
         ms_b = float(np.median(bt))
         batched = {"circuits_per_step": B, "ms_per_step": ms_b, "grads_per_s": B * 1e3 / ms_b,
+                   "autotune": tune_b,
                    "note": "B parameter sets of the same circuit in one batched plan (grid.z), gradient of the "
                            "summed loss w.r.t. every set's parameters"}
         del gb, circ_b
@@ -414,7 +432,8 @@ def gpu_arm(args, rank, world, cpu_base):
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 state / fp64 recurrences",
         "data": "synthetic seeded CV-QNN parameters and target",
         "config": _config({"fused_ops": nops, "wall_s_timed": round(wall, 3),
-                           "execution": "eager" if graphed is None else "one CUDA graph per step"}),
+                           "execution": "eager" if graphed is None else "one CUDA graph per step",
+                           "autotune": tune}),
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "kernels": kern,
         "grad_rel_err_vs_fp64": grad_err,
         "fd_baseline": {"gpu_forward_ms": 1e3 * fwd_s, "grads_per_s": fd_grads_per_s,
@@ -654,6 +673,7 @@ def main():
     ap.add_argument("--only", default="", help="single-gate case: comma-separated subset of the kernels")
     ap.add_argument("--modes", type=int, default=7, help="single-gate case: modes of the cutoff-12 ket")
     ap.add_argument("--eager", action="store_true", help="no CUDA graph capture")
+    ap.add_argument("--no-autotune", action="store_true", help="default kernel selection (no per-op tuning)")
     ap.add_argument("--batch", type=int, default=16,
                     help="gradient case: parameter sets per step of the extra batched-throughput line")
     args = ap.parse_args()

@@ -227,6 +227,19 @@ int fock_plan_backward_recompute(fock_plan* plan, const double* params, const vo
 int fock_plan_enable_timing(fock_plan* plan, int enable);
 int fock_plan_op_times(fock_plan* plan, float* fwd_ms, float* bwd_ms);
 
+/* Per-op kernel selection, the knobs of the autotuner
+ * (CompiledCircuit.autotune times each candidate with fock_plan_op_times and
+ * keeps the fastest per op).  family: 0 block kernels (one column per
+ * thread), 1 plane-tile kernels (two-mode ops whose plane geometry exists:
+ * `plane_ok`), -1 unchanged; adj_ctas_per_sm: CTAs per SM of the block
+ * adjoint launch (1..64; 0 unchanged; default 8).  Changes the partial-sum
+ * layout and so workspace_bytes (read fock_plan_get_info again and
+ * reallocate the workspace) and any captured graph of the plan.  Call with no
+ * sweep of the plan in flight.  No reference counterpart (the reference has
+ * one einsum per gate, tfbackend/ops.py:688-854). */
+int fock_plan_tune(fock_plan* plan, int op, int family, int adj_ctas_per_sm);
+int fock_plan_op_config(const fock_plan* plan, int op, int* family, int* adj_ctas_per_sm, int* plane_ok);
+
 /* Persistent sweeps.  A single-circuit complex64 plan whose state is at most
  * FOCK_GB300_SWEEP_MAX_BYTES bytes (read at plan creation; default 0 = off,
  * since per-op launches measured faster on GB300) runs a forward

@@ -207,6 +207,96 @@ class CompiledCircuit:
                 "fock_plan_backward_recompute")
         return grads, lam
 
+    def op_config(self, k):
+        """(family, adjoint CTAs per SM, plane_ok) of fused op k: family 0 is
+        the block kernels, 1 the plane-tile kernels."""
+        fam, ctas, ok = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        L.check(L.load().fock_plan_op_config(self._plan, int(k), ctypes.byref(fam), ctypes.byref(ctas),
+                                             ctypes.byref(ok)), "fock_plan_op_config")
+        return fam.value, ctas.value, bool(ok.value)
+
+    def tune_op(self, k, family=-1, ctas_per_sm=0):
+        """Select op k's kernel family (-1 keeps it) and block-adjoint CTAs
+        per SM (0 keeps it).  Reallocates the workspace on the next sweep;
+        graphs captured before the change are stale."""
+        torch.cuda.synchronize(self.device)
+        L.check(L.load().fock_plan_tune(self._plan, int(k), int(family), int(ctas_per_sm)), "fock_plan_tune")
+        info = L.PlanInfo()
+        L.check(L.load().fock_plan_get_info(self._plan, ctypes.byref(info)), "fock_plan_get_info")
+        self.info = info
+        self.release()
+
+    def _timed_sweeps(self, p, lam, repeats, per_op):
+        """Best-of-``repeats`` device times of one forward + adjoint sweep:
+        per op (fwd_ms, bwd_ms) arrays with ``per_op``, else the whole step in ms."""
+        lib = L.load()
+        n = self.n_ops
+        fbuf, bbuf = (ctypes.c_float * n)(), (ctypes.c_float * n)()
+        best_f, best_b, best = [float("inf")] * n, [float("inf")] * n, float("inf")
+        st = torch.cuda.current_stream(self.device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for r in range(repeats + 1):  # the first sweep warms up
+            e0.record(st)
+            states = self.forward_states(p)
+            self.backward(p, states, lam)
+            e1.record(st)
+            torch.cuda.synchronize(self.device)
+            if r == 0:
+                continue
+            best = min(best, e0.elapsed_time(e1))
+            if per_op:
+                L.check(lib.fock_plan_op_times(self._plan, fbuf, bbuf), "fock_plan_op_times")
+                best_f = [min(a, b) for a, b in zip(best_f, fbuf)]
+                best_b = [min(a, b) for a, b in zip(best_b, bbuf)]
+        return (best_f, best_b) if per_op else best
+
+    def autotune(self, params, ctas=(2, 4, 8, 16), repeats=3):
+        """Pick each op's kernel family and block-adjoint CTAs per SM by
+        timing a forward + adjoint sweep at ``params`` under every candidate
+        (per-op CUDA events, best of ``repeats``), keeping per op the
+        candidate with the smallest forward + adjoint time.  The tuned plan
+        is kept only when its whole step (PDL launches, final reduction) is
+        faster than the configuration it started from.  Returns
+        ``(configs, ms_before, ms_after)`` with configs[k] = (family, ctas)."""
+        if self.n_ops == 0:
+            return [], 0.0, 0.0
+        lib = L.load()
+        p = self._params(params)
+        g = torch.Generator(device="cpu").manual_seed(0)
+        lam = torch.complex(torch.randn(self._bshape, generator=g, dtype=torch.float64),
+                            torch.randn(self._bshape, generator=g, dtype=torch.float64))
+        lam = (lam / lam.abs().pow(2).sum().sqrt()).to(device=self.device, dtype=self.dtype)
+        n = self.n_ops
+        start = [self.op_config(k) for k in range(n)]
+        ms_before = self._timed_sweeps(p, lam, repeats, False)
+        cands = [(0, int(c)) for c in ctas]
+        if any(ok for _, _, ok in start):
+            cands.append((1, 0))
+        cost = [dict() for _ in range(n)]
+        L.check(lib.fock_plan_enable_timing(self._plan, 1), "fock_plan_enable_timing")
+        try:
+            for fam, c in cands:
+                for k in range(n):
+                    if fam == 0 or start[k][2]:
+                        self.tune_op(k, fam, c)
+                    else:
+                        self.tune_op(k, 0, start[k][1])
+                f, b = self._timed_sweeps(p, lam, repeats, True)
+                for k in range(n):
+                    if fam == 0 or start[k][2]:
+                        cost[k][(fam, c)] = f[k] + b[k]
+        finally:
+            L.check(lib.fock_plan_enable_timing(self._plan, 0), "fock_plan_enable_timing")
+        best = [min(ck, key=ck.get) for ck in cost]
+        for k, (fam, c) in enumerate(best):
+            self.tune_op(k, fam, c if fam == 0 else start[k][1])
+        ms_after = self._timed_sweeps(p, lam, repeats, False)
+        if ms_after > ms_before:
+            for k, (fam, c, _) in enumerate(start):
+                self.tune_op(k, fam, c)
+        self.tuned = [(fam, c) for fam, c, _ in (self.op_config(k) for k in range(n))]
+        return self.tuned, ms_before, min(ms_before, ms_after)
+
     def sweep_status(self):
         """(persistent, error): whether this plan runs its sweeps as single
         persistent launches, and whether a grid barrier of the last such sweep

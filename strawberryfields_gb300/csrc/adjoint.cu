@@ -68,17 +68,17 @@ static size_t adjoint_smem(int dtype, int D) {
   return (size_t)esz * ((size_t)((D * (D + 1) + 1) & ~1) + 2 * (size_t)rows * (tile_of(dtype) + 1));
 }
 
-AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout, int nb) {
+AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout, int nb, int ctas_per_sm) {
   AdjSched sc;
   memset(&sc, 0, sizeof(sc));
   sc.nblk = layout == LAYOUT_DENSE ? 1 : 2 * D - 1;
   if (sc.nblk > ADJ_MAX_BLOCKS) sc.nblk = 0;  // cutoff beyond FOCK_MAX_CUTOFF: callers reject it first
   const int64_t ntiles = (v.ncols + tile_of(dtype) - 1) / tile_of(dtype);
   // the same number of CTAs for every block (small blocks are memory-bound
-  // and need as many as large ones), about 8 CTAs per SM over all nb
+  // and need as many as large ones), ctas_per_sm CTAs per SM over all nb
   // circuits of a batch (grid.z); largest blocks come first in the flat grid
   // so they start first
-  const int target = std::max(1, 8 * fock_num_sms() / std::max(nb, 1));
+  const int target = std::max(1, std::max(ctas_per_sm, 1) * fock_num_sms() / std::max(nb, 1));
   int64_t part = 0;
   int start = 0;
   for (int y = 0; y < sc.nblk; ++y) {

@@ -209,8 +209,10 @@ struct AdjSched {
   int start[ADJ_MAX_BLOCKS + 1];
   int64_t part_off[ADJ_MAX_BLOCKS];
 };
-// nb: circuits of a batch launched together (grid.z)
-AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout, int nb = 1);
+// nb: circuits of a batch launched together (grid.z); ctas_per_sm: CTAs per
+// SM the launch spreads over all blocks and circuits (the default measured
+// best for the 6-mode cutoff-12 QNN; fock_plan_tune changes it per op)
+AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout, int nb = 1, int ctas_per_sm = 8);
 int launch_adjoint_partials(int dtype, const void* psi_in, const void* lam_out, void* lam_in,
                             const AxisView& v, int D, int layout, const double2* mat, int mflags,
                             double2* cpart, const AdjSched& sc, cudaStream_t st, const BatchArg& bt = BatchArg());

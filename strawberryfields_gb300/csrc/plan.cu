@@ -43,9 +43,11 @@ struct PlanOp {
   AdjSched sched;  // CTA schedule and partial-sum layout of the adjoint launch
   int64_t nent = 0;
   // plane-tile kernels (when the op fits them): geometry and persistent grids
-  int plane = 0;
+  int plane = 0;     // plane-tile kernels selected for this op
+  int plane_ok = 0;  // the plane geometry exists (fock_plan_tune may select it)
   PlaneGeom pg_fwd, pg_adj;
   int grid_fwd = 0, grid_adj = 0;
+  int adj_ctas = 8;  // adjoint CTAs per SM (block kernels)
   // persistent-sweep adjoint schedule and partial-sum region
   AdjSched psched;
   int64_t ppart_off = 0;
@@ -170,6 +172,43 @@ static void absorb_pending(PlanOp& op, int mode, std::vector<std::vector<Pending
     add_term(op, fn, 0, p.pidx);
   }
   pend[mode].clear();
+}
+
+// table of the one-launch reduction (in the pinned table image)
+static void write_red_table(fock_plan* P) {
+  RedOp* red = (RedOp*)(P->host + P->o_red);
+  for (size_t k = 0; k < P->ops.size(); ++k) {
+    const PlanOp& op = P->ops[k];
+    red[k].c_off = op.c_off;
+    red[k].cpart_off = op.cpart_off;
+    red[k].nent = (int)op.nent;
+    red[k].gx = op.plane ? op.grid_adj : op.sched.gx[0];
+    red[k].plane = op.plane;
+    red[k].layout = op.layout;
+  }
+}
+
+// Partial-sum regions and the workspace past the C arena: they depend on
+// every op's kernel family and adjoint schedule, so fock_plan_tune redoes them.
+static void layout_partials(fock_plan* P) {
+  int64_t sum = 0, mx = 0;
+  for (PlanOp& op : P->ops) {
+    const int64_t part_k = op.plane ? (int64_t)op.grid_adj * op.pg_adj.nent : op.sched.part_entries;
+    op.cpart_off = sum;
+    sum += part_k;
+    mx = std::max(mx, part_k);
+  }
+  // every op's partials kept until one reduction after the sweep when that
+  // costs at most 512 MiB (about 280 MB for the 6-mode cutoff-12 CV-QNN)
+  P->reduce_at_end = (double)sum * P->batch * sizeof(double2) <= 512.0 * (1 << 20);
+  P->cpart_entries = P->reduce_at_end ? sum : mx;
+  size_t o = align256(P->o_cpart + sizeof(double2) * std::max<int64_t>(P->cpart_entries, 1) * P->batch);
+  if (P->persist) {
+    P->o_sync = o; o = align256(o + (4 + P->ops.size()) * sizeof(unsigned));
+    P->o_ppart = o; o = align256(o + sizeof(double2) * std::max<int64_t>(P->ppart_entries, 1));
+  }
+  P->ws_bytes = o;
+  if (P->host) write_red_table(P);
 }
 
 extern "C" int fock_plan_create(int num_modes, int cutoff, int pure, int dtype, const fock_gate* gates,
@@ -385,7 +424,7 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
     P->persist = P->g_fwd > 0 && P->g_bwd > 0;
   }
   int64_t ppart = 0;
-  int64_t arena = 0, carena = 0, cpart = 0, cpart_sum = 0;
+  int64_t arena = 0, carena = 0;
   int n_terms = 0, n_contrib = 0;
   for (size_t k = 0; k < P->ops.size(); ++k) {
     PlanOp& op = P->ops[k];
@@ -409,13 +448,14 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
       op.swap = a > b;
       op.view = make_view2(naxes, D, std::min(a, b), std::max(a, b));
     }
-    op.sched = make_adj_sched(dtype, op.view, D, op.layout, batch);
-    op.plane = use_plane && (force_plane || plane_preferred(op.layout, op.view)) && make_plane_geom(dtype, op.view, D, op.layout, op.swap, 0, &op.pg_fwd) &&
-               make_plane_geom(dtype, op.view, D, op.layout, op.swap, 1, &op.pg_adj);
-    if (op.plane) {
+    op.sched = make_adj_sched(dtype, op.view, D, op.layout, batch, op.adj_ctas);
+    op.plane_ok = use_plane && make_plane_geom(dtype, op.view, D, op.layout, op.swap, 0, &op.pg_fwd) &&
+                  make_plane_geom(dtype, op.view, D, op.layout, op.swap, 1, &op.pg_adj);
+    if (op.plane_ok) {
       op.grid_fwd = plane_grid(dtype, op.pg_fwd, 0, batch);
       op.grid_adj = plane_grid(dtype, op.pg_adj, 1, batch);
     }
+    op.plane = op.plane_ok && (force_plane || plane_preferred(op.layout, op.view));
     if (P->persist) {
       op.psched = make_adj_sched_grid(dtype, op.view, D, op.layout, P->g_bwd);
       op.ppart_off = ppart;
@@ -423,10 +463,6 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
     }
     op.c_off = carena;
     carena += op.nent;
-    const int64_t part_k = op.plane ? (int64_t)op.grid_adj * op.pg_adj.nent : op.sched.part_entries;
-    op.cpart_off = cpart_sum;
-    cpart_sum += part_k;
-    cpart = std::max<int64_t>(cpart, part_k);
     n_terms += (int)op.terms.size();
     n_contrib += (int)op.contribs.size();
     // flops: 8 real flops per complex multiply-add
@@ -435,10 +471,6 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   }
   P->arena_entries = arena;
   P->carena_entries = carena;
-  // every op's partials kept until one reduction after the sweep when that
-  // costs at most 512 MiB (about 280 MB for the 6-mode cutoff-12 CV-QNN)
-  P->reduce_at_end = (double)cpart_sum * batch * sizeof(double2) <= 512.0 * (1 << 20);
-  P->cpart_entries = P->reduce_at_end ? cpart_sum : cpart;
   P->n_terms = n_terms;
   P->n_contrib = n_contrib;
   const int n_ops = (int)P->ops.size();
@@ -456,13 +488,9 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   P->tables_bytes = o;
   P->o_arena = o; o = align256(o + sizeof(double2) * arena * batch);
   P->o_carena = o; o = align256(o + sizeof(double2) * std::max<int64_t>(carena, 1) * batch);
-  P->o_cpart = o; o = align256(o + sizeof(double2) * std::max<int64_t>(P->cpart_entries, 1) * batch);
-  if (P->persist) {
-    P->ppart_entries = ppart;
-    P->o_sync = o; o = align256(o + (4 + n_ops) * sizeof(unsigned));
-    P->o_ppart = o; o = align256(o + sizeof(double2) * std::max<int64_t>(ppart, 1));
-  }
-  P->ws_bytes = o;
+  P->o_cpart = o;
+  P->ppart_entries = ppart;
+  layout_partials(P);
 
   if (cudaHostAlloc((void**)&P->host, P->tables_bytes, cudaHostAllocDefault) != cudaSuccess) {
     // fall back to pageable memory (copies are then synchronous)
@@ -510,16 +538,7 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
       ++c;
     }
   }
-  RedOp* red = (RedOp*)(P->host + P->o_red);
-  for (int k = 0; k < n_ops; ++k) {
-    const PlanOp& op = P->ops[k];
-    red[k].c_off = op.c_off;
-    red[k].cpart_off = op.cpart_off;
-    red[k].nent = (int)op.nent;
-    red[k].gx = op.plane ? op.grid_adj : op.sched.gx[0];
-    red[k].plane = op.plane;
-    red[k].layout = op.layout;
-  }
+  write_red_table(P);
   if (P->persist) {
     SweepOp* sw_ops = (SweepOp*)(P->host + P->o_sweep);
     for (int k = 0; k < n_ops; ++k) {
@@ -882,6 +901,31 @@ extern "C" int fock_plan_backward_recompute(fock_plan* P, const double* params, 
   }
   if (lam != grad_state) FOCK_CUDA_TRY(cudaMemcpyAsync(grad_state, lam, c.sb, cudaMemcpyDeviceToDevice, st));
   return param_grads(P, ws, c, grad_params, st);
+}
+
+extern "C" int fock_plan_tune(fock_plan* P, int k, int family, int adj_ctas_per_sm) {
+  if (!P || k < 0 || k >= (int)P->ops.size()) return fock_set_error(FOCK_ERR_INVALID, "bad op index");
+  PlanOp& op = P->ops[k];
+  if (family > 1) return fock_set_error(FOCK_ERR_INVALID, "kernel family must be 0 (block) or 1 (plane)");
+  if (family == 1 && !op.plane_ok) return fock_set_error(FOCK_ERR_UNSUPPORTED, "op %d has no plane-tile kernel", k);
+  if (adj_ctas_per_sm < 0 || adj_ctas_per_sm > 64)
+    return fock_set_error(FOCK_ERR_INVALID, "adjoint CTAs per SM must be in [1, 64]");
+  if (family >= 0) op.plane = family;
+  if (adj_ctas_per_sm > 0) {
+    op.adj_ctas = adj_ctas_per_sm;
+    op.sched = make_adj_sched(P->dtype, op.view, P->D, op.layout, P->batch, adj_ctas_per_sm);
+  }
+  layout_partials(P);
+  return FOCK_OK;
+}
+
+extern "C" int fock_plan_op_config(const fock_plan* P, int k, int* family, int* adj_ctas_per_sm, int* plane_ok) {
+  if (!P || k < 0 || k >= (int)P->ops.size()) return fock_set_error(FOCK_ERR_INVALID, "bad op index");
+  const PlanOp& op = P->ops[k];
+  if (family) *family = op.plane;
+  if (adj_ctas_per_sm) *adj_ctas_per_sm = op.adj_ctas;
+  if (plane_ok) *plane_ok = op.plane_ok;
+  return FOCK_OK;
 }
 
 extern "C" int fock_plan_sweep_status(const fock_plan* P, const void* workspace, int* grids, int* error) {

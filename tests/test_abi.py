@@ -163,6 +163,45 @@ def test_mixed_plan_structure(lib):
     lib.fock_plan_destroy(plan)
 
 
+def test_plan_tune_knobs(lib):
+    """fock_plan_tune: per-op kernel family and adjoint CTA density, argument
+    checks, and the workspace it implies (more adjoint CTAs, more partials)."""
+    from strawberryfields_gb300 import _lib
+    from strawberryfields_gb300.qnn import qnn_gates
+
+    gates, npar = qnn_gates(6, 1)
+    rc, plan = _plan(gates, npar, N=6, D=10)
+    assert rc == 0
+    info, ops = _ops(plan)
+
+    def cfg(k):
+        f, c, ok = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        assert lib.fock_plan_op_config(plan, k, ctypes.byref(f), ctypes.byref(c), ctypes.byref(ok)) == 0
+        return f.value, c.value, ok.value
+
+    configs = [cfg(k) for k in range(info.n_ops)]
+    assert all(c == 8 for _, c, _ in configs)
+    assert any(ok for _, _, ok in configs)
+    assert lib.fock_plan_tune(plan, 0, 2, 0) == _lib.FOCK_ERR_INVALID
+    assert lib.fock_plan_tune(plan, 0, -1, 65) == _lib.FOCK_ERR_INVALID
+    assert lib.fock_plan_tune(plan, info.n_ops, -1, 4) == _lib.FOCK_ERR_INVALID
+    ws0 = info.workspace_bytes
+    sizes = []
+    for ctas in (2, 16):
+        for k in range(info.n_ops):
+            assert lib.fock_plan_tune(plan, k, 0, ctas) == 0
+        sizes.append(_ops(plan)[0].workspace_bytes)
+    assert sizes[1] > sizes[0] and cfg(0)[:2] == (0, 16)
+    for k in range(info.n_ops):
+        assert lib.fock_plan_tune(plan, k, configs[k][0], configs[k][1]) == 0
+    assert _ops(plan)[0].workspace_bytes == ws0
+    lib.fock_plan_destroy(plan)
+    # two-mode plane tiles stop at cutoff 16: a cutoff-18 beamsplitter has none
+    rc, plan = _plan([(5, 0, 1, 0)], 2, N=2, D=18)
+    assert rc == 0 and lib.fock_plan_tune(plan, 0, 1, 0) == _lib.FOCK_ERR_UNSUPPORTED
+    lib.fock_plan_destroy(plan)
+
+
 def test_product_path_has_no_cpu_fallback():
     """The package never imports the oracle."""
     pkg = os.path.join(ROOT, "strawberryfields_gb300")

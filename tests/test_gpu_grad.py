@@ -275,3 +275,35 @@ def test_backward_reuses_or_rebuilds_matrices(cuda):
     s1 = c.forward_states(p1)
     p1.mul_(1.0)  # in-place update: version changes, matrices rebuilt
     assert torch.allclose(c.backward(p1, s1, g_state)[0], ref1, rtol=1e-12, atol=1e-14)
+
+
+def test_tuned_kernels_give_the_same_gradient(cuda):
+    """Every kernel family and adjoint CTA density of fock_plan_tune, and the
+    autotuner's pick, give the untuned gradient (complex128: only the order
+    of the partial sums changes)."""
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+    from strawberryfields_gb300.qnn import qnn_gates, qnn_params
+
+    N, D = 4, 9
+    gates, npar = qnn_gates(N, 2)
+    p = torch.tensor(qnn_params(gates, npar, seed=3), device="cuda")
+    g_state = torch.randn([D] * N, dtype=torch.complex128, device="cuda")
+    c = CompiledCircuit(N, D, gates, npar, dtype=torch.complex128)
+    ref_s = c.forward_states(p)
+    ref_g = c.backward(p, ref_s, g_state)[0]
+    start = [c.op_config(k) for k in range(c.n_ops)]
+    assert any(ok for _, _, ok in start)
+    for fam, ctas in [(0, 1), (0, 3), (0, 16), (1, 0)]:
+        for k in range(c.n_ops):
+            c.tune_op(k, fam if (fam == 0 or start[k][2]) else 0, ctas)
+        s = c.forward_states(p)
+        assert torch.allclose(s, ref_s, rtol=0, atol=1e-13), (fam, ctas)
+        g = c.backward(p, s, g_state)[0]
+        assert torch.allclose(g, ref_g, rtol=1e-11, atol=1e-13), (fam, ctas)
+    configs, before, after = c.autotune(p, ctas=(2, 8), repeats=1)
+    assert len(configs) == c.n_ops and after <= before
+    s = c.forward_states(p)
+    g = c.backward(p, s, g_state)[0]
+    assert torch.allclose(s, ref_s, rtol=0, atol=1e-13)
+    assert torch.allclose(g, ref_g, rtol=1e-11, atol=1e-13)
