@@ -227,6 +227,15 @@ int fock_plan_backward_recompute(fock_plan* plan, const double* params, const vo
 int fock_plan_enable_timing(fock_plan* plan, int enable);
 int fock_plan_op_times(fock_plan* plan, float* fwd_ms, float* bwd_ms);
 
+/* Wigner function of one mode on a grid: BaseFockState.wigner
+ * (strawberryfields/backends/states.py:730-785).  rho: the mode's D x D
+ * reduced density matrix, complex128 on the device (fock_reduced_dm1);
+ * xvec[nx], pvec[np]: device float64 grids; out: device float64 [np][nx],
+ * out[i][j] = W(xvec[j], pvec[i]) (the reference's meshgrid order), for the
+ * quadratures x = sqrt(hbar/2)(a + a^dagger).  FP64 throughout. */
+int fock_wigner(int cutoff, const void* rho, const double* xvec, int nx, const double* pvec, int np,
+                double hbar, double* out, void* stream);
+
 /* Per-op kernel selection, the knobs of the autotuner
  * (CompiledCircuit.autotune times each candidate with fock_plan_op_times and
  * keeps the fastest per op).  family: 0 block kernels (one column per

@@ -25,7 +25,7 @@ What it restates (complex128 / FP64 throughout, like the reference):
   the reference's per-fibre Python loops (same arithmetic, same index order);
 * readouts of ``strawberryfields/backends/states.py`` (``all_fock_probs`` :580,
   ``fock_prob`` :644, ``reduced_dm`` :613, ``mean_photon`` :657) computed from
-  marginals instead of the full density matrix.
+  marginals instead of the full density matrix, and ``wigner`` :730.
 
 Parity of these restatements is pinned by ``tests/test_oracle.py`` against
 ``scipy.linalg.expm`` of each gate generator, against the reference's own
@@ -538,6 +538,36 @@ def homodyne_pdf(rho, phi, hbar=2.0, q_max=10.0, num_bins=100000):
         for b in range(D):
             dist += r[a, b] * H[a] * H[b] / math.sqrt(2 ** a * math.factorial(a) * 2 ** b * math.factorial(b))
     return q, (dist * np.sqrt(mw / np.pi) * np.exp(-mw * q ** 2) * (q[1] - q[0])).real
+
+
+def wigner(rho, xvec, pvec, hbar=2.0):
+    """Wigner function of a single-mode density matrix on the grid
+    meshgrid(xvec, pvec) (shape [len(pvec), len(xvec)]): the reference's
+    iterative evaluation (strawberryfields/backends/states.py:730-785).
+    Grids G[n] for |m><n| are filled row by row, m = 0 first:
+    G[n] = 2 A G[n-1] / sqrt(n) on row 0, then on row m the diagonal entry
+    (2 conj(A) G[m] - sqrt(m) G[m-1]) / sqrt(m) and the entries right of it
+    (2 A G[n-1] - sqrt(m) G_prev[n]) / sqrt(n), G_prev being row m-1; W sums
+    Re rho[m][m] G[m] + 2 Re rho[m][n] G[n] (n > m) and is divided by hbar."""
+    D = rho.shape[0]
+    Q, P = np.meshgrid(np.asarray(xvec, dtype=float), np.asarray(pvec, dtype=float))
+    A = (Q + 1j * P) / (2 * np.sqrt(hbar / 2))
+    G = [np.exp(-2.0 * np.abs(A) ** 2) / np.pi + 0j]
+    W = np.real(rho[0, 0]) * np.real(G[0])
+    for n in range(1, D):
+        G.append(2.0 * A * G[n - 1] / np.sqrt(n))
+        W = W + 2 * np.real(rho[0, n] * G[n])
+    for m in range(1, D):
+        prev_m = G[m].copy()
+        G[m] = (2 * np.conj(A) * prev_m - np.sqrt(m) * G[m - 1]) / np.sqrt(m)
+        W = W + np.real(rho[m, m] * G[m])
+        prev = prev_m
+        for n in range(m + 1, D):
+            new = (2 * A * G[n - 1] - np.sqrt(m) * prev) / np.sqrt(n)
+            prev = G[n].copy()
+            G[n] = new
+            W = W + 2 * np.real(rho[m, n] * G[n])
+    return W / hbar
 
 
 def homodyne_project(state, phi, x, mode, n, pure=True, hbar=2.0):

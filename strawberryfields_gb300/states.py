@@ -53,6 +53,18 @@ class FockStateGB300:
     def __str__(self):
         return self._str
 
+    def __eq__(self, other):
+        """Equal when the other state is of this type, has the same modes and
+        shape, and the density matrices agree within EQ_TOLERANCE
+        (states.py:503-526)."""
+        if not isinstance(other, type(self)):
+            return False
+        if self._modes != other._modes or tuple(self._tensor.shape) != tuple(other._tensor.shape):
+            return False
+        return bool(np.allclose(self.dm(), other.dm(), atol=self.EQ_TOLERANCE, rtol=0))
+
+    __hash__ = object.__hash__
+
     __repr__ = __str__
 
     # ----------------------------------------------------------------- basics
@@ -148,7 +160,8 @@ class FockStateGB300:
         var = float(np.sum(k * k * p) - mean ** 2)
         return mean, var
 
-    def _rdm1(self, mode):
+    def _rdm1_dev(self, mode):
+        """One mode's reduced density matrix, complex128 device tensor [D, D]."""
         D, n = self._cutoff, self._modes
         out = torch.empty((D, D), dtype=torch.complex128, device=self._tensor.device)
         lib = L.load()
@@ -156,7 +169,10 @@ class FockStateGB300:
                          dtype=torch.uint8, device=self._tensor.device)
         L.call("fock_reduced_dm1", n, D, int(self._pure), self._dcode, mode, self._tensor.data_ptr(),
                out.data_ptr(), ws.data_ptr(), torch.cuda.current_stream(self._tensor.device).cuda_stream)
-        return out.cpu().numpy()
+        return out
+
+    def _rdm1(self, mode):
+        return self._rdm1_dev(mode).cpu().numpy()
 
     def reduced_dm(self, modes, **kwargs):
         """Reduced density matrix (states.py:613).  One mode: device
@@ -240,6 +256,93 @@ class FockStateGB300:
         mean = np.trace(np.dot(xphi, rho)).real
         var = np.trace(np.dot(xphisq, rho)).real - mean ** 2
         return float(mean), float(var)
+
+    def wigner(self, mode, xvec, pvec):
+        """Discretised Wigner function of one mode (states.py:730): array
+        [len(pvec), len(xvec)] with entry [i, j] at (xvec[j], pvec[i]),
+        evaluated on the device from the mode's reduced density matrix."""
+        rho = self._rdm1_dev(mode)
+        dev = rho.device
+        xv = torch.as_tensor(np.asarray(xvec, dtype=np.float64).reshape(-1), device=dev)
+        pv = torch.as_tensor(np.asarray(pvec, dtype=np.float64).reshape(-1), device=dev)
+        out = torch.empty((pv.numel(), xv.numel()), dtype=torch.float64, device=dev)
+        L.call("fock_wigner", self._cutoff, rho.data_ptr(), xv.data_ptr(), xv.numel(), pv.data_ptr(), pv.numel(),
+               float(self._hbar), out.data_ptr(), torch.cuda.current_stream(dev).cuda_stream)
+        return out.cpu().numpy()
+
+    def p_quad_values(self, mode, xvec, pvec):
+        """p-quadrature distribution on ``pvec`` (states.py:436): the Wigner
+        function integrated over ``xvec`` by Simpson's rule."""
+        from scipy.integrate import simpson
+
+        W = self.wigner(mode, xvec, pvec)
+        return np.array([simpson(W[i, : len(xvec)], x=xvec) for i in range(len(pvec))])
+
+    def x_quad_values(self, mode, xvec, pvec):
+        """x-quadrature distribution on ``xvec`` (states.py:456): the Wigner
+        function integrated over ``pvec`` by Simpson's rule."""
+        from scipy.integrate import simpson
+
+        W = self.wigner(mode, xvec, pvec)
+        return np.array([simpson(W[: len(pvec), i], x=pvec) for i in range(len(xvec))])
+
+    def poly_quad_expectation(self, A, d=None, k=0, phi=0, **kwargs):
+        """Mean and variance of the quadrature polynomial
+        Q = r^T A r + d^T r + k, r = (x_1..x_N, p_1..p_N) rotated by ``phi``
+        (x_phi = x cos phi + p sin phi, p_phi = -x sin phi + p cos phi), as
+        the reference evaluates it (states.py:806-945): the operators are
+        built in the Fock basis with cutoff D + 1, Q and Q^2 formed there and
+        truncated to D, then traced against the reduced density matrix of the
+        modes the coefficients touch."""
+        N, D = self._modes, self._cutoff
+        A = np.zeros([2 * N, 2 * N]) if A is None else np.asarray(A)
+        if A.shape != (2 * N, 2 * N):
+            raise ValueError("Matrix of quadratic coefficients A must be of size 2Nx2N.")
+        if not np.allclose(A.T, A):
+            raise ValueError("Matrix of quadratic coefficients A must be symmetric.")
+        d = np.zeros([2 * N]) if d is None else np.asarray(d)
+        if d.shape != (2 * N,):
+            raise ValueError("Vector of linear coefficients d must be of length 2N.")
+        modes = sorted({int(i) % N for i in A.nonzero()[0]} | {int(i) % N for i in d.nonzero()[0]})
+        if not modes:
+            return k, 0.0
+        km = len(modes)
+        dim = D + 1
+        a = np.diag(np.sqrt(np.arange(1, dim)), 1)
+        x0 = np.sqrt(self._hbar / 2) * (a + a.T)
+        p0 = -1j * np.sqrt(self._hbar / 2) * (a - a.T)
+        xr = np.cos(phi) * x0 + np.sin(phi) * p0
+        pr = -np.sin(phi) * x0 + np.cos(phi) * p0
+
+        def on_mode(op, q):
+            out = np.ones((1, 1))
+            for j in range(km):
+                out = np.kron(out, op if j == q else np.eye(dim))
+            return out
+
+        r = [on_mode(xr, q) for q in range(km)] + [on_mode(pr, q) for q in range(km)]
+        idx = modes + [N + m for m in modes]
+        Aq = A[np.ix_(idx, idx)]
+        op = np.zeros((dim ** km, dim ** km), dtype=np.complex128)
+        for i in range(2 * km):
+            row = sum(Aq[i, j] * r[j] for j in range(2 * km) if Aq[i, j] != 0)
+            if not np.isscalar(row):
+                op += r[i] @ row
+            if d[idx[i]] != 0:
+                op += d[idx[i]] * r[i]
+        if k != 0:
+            op += k * np.eye(dim ** km)
+        op2 = op @ op
+
+        def truncate(M):
+            return M.reshape([dim] * (2 * km))[(slice(0, D),) * (2 * km)].reshape(D ** km, D ** km)
+
+        rho = np.asarray(self.reduced_dm(modes))
+        # interleaved [o0, i0, o1, i1, ...] -> matrix [(o0 o1 ..), (i0 i1 ..)]
+        rho = rho.transpose([2 * q for q in range(km)] + [2 * q + 1 for q in range(km)]).reshape(D ** km, D ** km)
+        mean = float(np.real(np.trace(truncate(op) @ rho)))
+        var = float(np.real(np.trace(truncate(op2) @ rho)) - mean ** 2)
+        return mean, var
 
     def number_expectation(self, modes):
         values = np.arange(self._cutoff)

@@ -217,3 +217,85 @@ def test_oracle_homodyne_pdf_coherent_state():
         assert abs(np.sum(p) - 1) < 1e-6
         assert abs(mean - 2 * 0.8 * np.cos(0.5 - phi)) < 1e-8
         assert abs(var - 1.0) < 1e-8
+
+
+def _readout_cases():
+    d = os.path.join(GOLDEN, "readouts")
+    return sorted(f[:-4] for f in os.listdir(d) if f.endswith(".npz"))
+
+
+@pytest.mark.parametrize("case", _readout_cases())
+def test_oracle_wigner_reproduces_golden(case):
+    """The oracle's Wigner iteration against the reference's own
+    BaseFockState.wigner on the reduced states of a golden circuit."""
+    r = np.load(os.path.join(GOLDEN, "readouts", case + ".npz"))
+    z = np.load(os.path.join(GOLDEN, str(r["source"]) + ".npz"))
+    N = int(z["N"])
+    for i, m in enumerate(r["wigner_modes"]):
+        rho = fo.reduced_dm(z["state"], N, int(m), bool(z["out_pure"]))
+        W = fo.wigner(rho, r["xvec"], r["pvec"], float(r["hbar"]))
+        assert np.abs(W - r["wigner"][i]).max() < 1e-14
+
+
+def test_oracle_wigner_gaussian_known_answers():
+    """Vacuum and coherent states: normal distributions with covariance
+    hbar/2 and mean sqrt(2 hbar) (Re alpha, Im alpha) (the reference's
+    tests/backend/test_states_wigner.py:55-110)."""
+    from scipy.stats import multivariate_normal
+
+    D, hbar = 30, 1.7
+    xv = np.linspace(-4, 4, 33)
+    X, P = np.meshgrid(xv, xv)
+    grid = np.stack([X, P], axis=-1)
+    for alpha in (0.0, 0.5 + 0.3j):
+        psi = fo.coherent_state(abs(alpha), np.angle(alpha), D)
+        W = fo.wigner(np.outer(psi, psi.conj()), xv, xv, hbar)
+        mu = np.sqrt(2 * hbar) * np.array([alpha.real, alpha.imag])
+        exact = multivariate_normal(mu, np.eye(2) * hbar / 2).pdf(grid)
+        assert np.abs(W - exact).max() < 1e-12
+
+
+class _HostState:
+    """The readout host logic of FockStateGB300 on a numpy state, with the
+    device reductions replaced by the oracle's (no GPU)."""
+
+    def __init__(self, state, N, D, pure, hbar):
+        from strawberryfields_gb300.states import FockStateGB300
+
+        self.s = object.__new__(FockStateGB300)
+        self.s._modes, self.s._cutoff, self.s._pure, self.s._hbar = N, D, pure, hbar
+        self.state = state
+
+        def reduced_dm(modes, **kwargs):
+            modes = [modes] if isinstance(modes, int) else list(modes)
+            if len(modes) == 1:
+                return fo.reduced_dm(state, N, modes[0], pure)
+            rho = state if not pure else fo.mix(state, N)
+            for m in sorted(set(range(N)) - set(modes), reverse=True):
+                rho = np.trace(rho, axis1=2 * m, axis2=2 * m + 1)
+            return rho
+
+        self.s.reduced_dm = reduced_dm
+
+
+@pytest.mark.parametrize("case", _readout_cases())
+def test_poly_quad_expectation_host_logic_matches_golden(case):
+    r = np.load(os.path.join(GOLDEN, "readouts", case + ".npz"))
+    z = np.load(os.path.join(GOLDEN, str(r["source"]) + ".npz"))
+    h = _HostState(z["state"], int(z["N"]), int(z["D"]), bool(z["out_pure"]), float(r["hbar"]))
+    for i in range(len(r["poly_k"])):
+        A = None if r["poly_A_none"][i] else r["poly_A"][i]
+        d = None if r["poly_d_none"][i] else r["poly_d"][i]
+        got = h.s.poly_quad_expectation(A, d, float(r["poly_k"][i]), phi=float(r["poly_phi"][i]))
+        assert np.allclose(got, r["poly_mean_var"][i], rtol=1e-12, atol=1e-12), (case, i)
+
+
+def test_poly_quad_expectation_argument_checks():
+    h = _HostState(fo.vacuum(2, 4), 2, 4, True, 2.0)
+    with pytest.raises(ValueError, match="2Nx2N"):
+        h.s.poly_quad_expectation(np.eye(3))
+    with pytest.raises(ValueError, match="symmetric"):
+        h.s.poly_quad_expectation(np.triu(np.ones((4, 4))))
+    with pytest.raises(ValueError, match="length 2N"):
+        h.s.poly_quad_expectation(np.eye(4), np.ones(3))
+    assert h.s.poly_quad_expectation(None, None, 2.5) == (2.5, 0.0)
