@@ -65,7 +65,7 @@ static size_t adjoint_smem(int dtype, int D) {
   const int esz = dtype == FOCK_C64 ? 8 : 16;
   const int rows = 4 * ((D + 3) / 4);
   // matrix + the lam and psi tiles
-  return (size_t)esz * ((size_t)((D * (D + 1) + 1) & ~1) + 2 * (size_t)rows * (tile_of(dtype) + 1));
+  return (size_t)esz * (((ms_slots(dtype, D) + 1) & ~(size_t)1) + 2 * (size_t)rows * (tile_of(dtype) + 1));
 }
 
 AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout, int nb, int ctas_per_sm) {

@@ -75,7 +75,7 @@ static int launch_apply_t(const void* in, void* out, const AxisView& v, int D, i
   if (gx > 0x7fffffffLL) return fock_set_error(FOCK_ERR_INVALID, "state too large");
   if (bt.nb < 1 || bt.nb > 65535) return fock_set_error(FOCK_ERR_INVALID, "batch of %d circuits", bt.nb);
   dim3 grid((unsigned)gx, nblk, bt.nb);
-  const size_t sm = (size_t)D * (D + 1) * sizeof(CT);  // rows padded to even length
+  const size_t sm = ms_slots(sizeof(CT) == 8 ? FOCK_C64 : FOCK_C128, D) * sizeof(CT);
   auto k = apply_block_kernel<CT, DMAX>;
   if (sm > 48 * 1024) FOCK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   FOCK_CUDA_TRY(launch_kernel(k, grid, dim3(APPLY_THREADS), sm, st, bt.pdl, (const CT*)in, (CT*)out, v, D, layout,

@@ -113,6 +113,9 @@ __host__ __device__ __forceinline__ int ms_stride(int s) {
   return sizeof(CT) == 8 ? (s + 1) & ~1 : s;
 }
 
+// state-type slots the staged block of a cutoff-D op needs
+__host__ __device__ __forceinline__ size_t ms_slots(int, int D) { return (size_t)D * (D + 1); }
+
 // Stage the s x s block for this CTA into shared memory in the state precision,
 // as the matrix that maps the view's input positions to its output positions
 // (row w at Ms + w * ms_stride(s)).
@@ -131,22 +134,59 @@ __device__ __forceinline__ void stage_block(CT* Ms, const double2* mat, const Bl
   }
 }
 
+// A column of s values held in registers in the form the row products use.
+// complex64: each value x as the pairs (Re x, Re x) and (Im x, Im x), so a
+// row product is two paired FMAs per entry with the staged entry (Re m, Im m)
+// as the other operand -- P += m * Re x, Q += m * Im x, and
+// m x = (P.re - Q.im, P.im + Q.re) -- half the FP32 instructions of the scalar
+// complex FMA; the pairs are built once per column and reused by all s rows.
+// (Measured on GB300 against the scalar form and against expanding the staged
+// entries instead, which doubles the shared-memory loads: the dense apply at
+// 12^7 went from 106 to 96 us and the last-pair beamsplitter from 199 to
+// 154 us, the 6-mode cutoff-12 QNN gradient from 8.09 to 7.63 ms.)
+template <typename CT, int S> struct ColRegs;
+template <int S> struct ColRegs<double2, S> {
+  double2 x[S];
+  __device__ __forceinline__ void set(const double2 (&v)[S]) {
+#pragma unroll
+    for (int u = 0; u < S; ++u) x[u] = v[u];
+  }
+};
+template <int S> struct ColRegs<float2, S> {
+  f32x2 re[S], im[S];
+  __device__ __forceinline__ void set(const float2 (&v)[S]) {
+#pragma unroll
+    for (int u = 0; u < S; ++u) {
+      re[u] = pk2(v[u].x, v[u].x);
+      im[u] = pk2(v[u].y, v[u].y);
+    }
+  }
+};
+
 // a += sum_u row[u] x[u] over one staged row (16-byte loads of entry pairs
 // for complex64; rows start on 16-byte boundaries)
 template <int S>
-__device__ __forceinline__ void row_mac(float2& a, const float2* row, const float2 (&x)[S]) {
-  const float4* r4 = reinterpret_cast<const float4*>(row);
+__device__ __forceinline__ void row_mac(float2& a, const float2* row, const ColRegs<float2, S>& x) {
+  const ulonglong2* r2 = reinterpret_cast<const ulonglong2*>(row);
+  f32x2 P = 0ull, Q = 0ull;
 #pragma unroll
   for (int u2 = 0; u2 < (S + 1) / 2; ++u2) {
-    const float4 m = r4[u2];
-    cfma(a, make_float2(m.x, m.y), x[2 * u2]);
-    if (2 * u2 + 1 < S) cfma(a, make_float2(m.z, m.w), x[2 * u2 + 1]);
+    const ulonglong2 m = r2[u2];
+    P = ffma2(m.x, x.re[2 * u2], P);
+    Q = ffma2(m.x, x.im[2 * u2], Q);
+    if (2 * u2 + 1 < S) {
+      P = ffma2(m.y, x.re[2 * u2 + 1], P);
+      Q = ffma2(m.y, x.im[2 * u2 + 1], Q);
+    }
   }
+  const float2 p = upk2(P), q = upk2(Q);
+  a.x += p.x - q.y;
+  a.y += p.y + q.x;
 }
 template <int S>
-__device__ __forceinline__ void row_mac(double2& a, const double2* row, const double2 (&x)[S]) {
+__device__ __forceinline__ void row_mac(double2& a, const double2* row, const ColRegs<double2, S>& x) {
 #pragma unroll
-  for (int u = 0; u < S; ++u) cfma(a, row[u], x[u]);
+  for (int u = 0; u < S; ++u) cfma(a, row[u], x.x[u]);
 }
 
 // A batch of nb independent circuits of one structure: grid.z indexes the

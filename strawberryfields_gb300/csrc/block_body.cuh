@@ -41,10 +41,14 @@ __device__ __forceinline__ void apply_cols(const CT* __restrict__ in, CT* __rest
   __syncthreads();
   if (!valid) return;
   constexpr int SP = sizeof(CT) == 8 ? (S + 1) & ~1 : S;
-#pragma unroll
+  ColRegs<CT, S> xc;
+  xc.set(x0);
+  // rows one at a time: unrolled, the loads of later rows run ahead and
+  // spill the column's registers
+#pragma unroll 1
   for (int w = 0; w < S; ++w) {
     CT a0 = czero<CT>();
-    row_mac<S>(a0, Ms + w * SP, x0);
+    row_mac<S>(a0, Ms + w * SP, xc);
     out[b0 + w * g.step] = a0;
   }
 }
@@ -157,10 +161,12 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
       CT lam[S];
 #pragma unroll
       for (int u = 0; u < S; ++u) lam[u] = lam_s[u * LD + tid];
-#pragma unroll
+      ColRegs<CT, S> lc;
+      lc.set(lam);
+#pragma unroll 1
       for (int w = 0; w < S; ++w) {
         CT a = czero<CT>();
-        row_mac<S>(a, MsH + w * SP, lam);
+        row_mac<S>(a, MsH + w * SP, lc);
         lam_in[base + w * g.step] = a;
       }
     }

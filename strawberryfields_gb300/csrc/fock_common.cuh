@@ -50,6 +50,28 @@ template <typename C> __host__ __device__ __forceinline__ void cfma_conj(C& acc,
 }
 template <typename C, typename S> __host__ __device__ __forceinline__ C cscale(C a, S s) { a.x *= s; a.y *= s; return a; }
 
+// Packed FP32 pairs for the Blackwell paired FMA (fma.rn.f32x2: one
+// instruction, two lanes, each rounded like a scalar fma).  A pair lives in a
+// 64-bit register (low lane first), so a complex64 entry loaded from memory
+// is already a pair.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float lo, float hi) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float2 upk2(f32x2 v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+// a * b + c, lane by lane
+__device__ __forceinline__ f32x2 ffma2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
 __device__ __forceinline__ float2 to_c(double2 v, float2*) { return make_float2((float)v.x, (float)v.y); }
 __device__ __forceinline__ double2 to_c(double2 v, double2*) { return v; }
 __device__ __forceinline__ double2 to_d(float2 v) { return make_double2(v.x, v.y); }

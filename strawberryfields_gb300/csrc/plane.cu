@@ -160,18 +160,41 @@ __device__ __forceinline__ void pl_stage(CT* Ms, const double2* __restrict__ mat
   }
 }
 
-// one column's block: x = Ms x in place (positions base + u*step)
+// one column's block: x = Ms x in place (positions base + u*step); complex64
+// with paired FMAs (the column as (Re, Re) / (Im, Im) pairs, entries read as
+// pairs)
 template <typename CT, int S>
 __device__ __forceinline__ void pl_block(CT* row, int base, int step, const CT* Ms) {
   CT x[S];
 #pragma unroll
   for (int u = 0; u < S; ++u) x[u] = row[base + u * step];
+  if constexpr (sizeof(CT) == 8) {
+    f32x2 re[S], im[S];
 #pragma unroll
-  for (int w = 0; w < S; ++w) {
-    CT a = czero<CT>();
+    for (int u = 0; u < S; ++u) {
+      re[u] = pk2(x[u].x, x[u].x);
+      im[u] = pk2(x[u].y, x[u].y);
+    }
 #pragma unroll
-    for (int u = 0; u < S; ++u) cfma(a, Ms[w * S + u], x[u]);
-    row[base + w * step] = a;
+    for (int w = 0; w < S; ++w) {
+      const f32x2* m = reinterpret_cast<const f32x2*>(Ms + w * S);
+      f32x2 P = 0ull, Q = 0ull;
+#pragma unroll
+      for (int u = 0; u < S; ++u) {
+        P = ffma2(m[u], re[u], P);
+        Q = ffma2(m[u], im[u], Q);
+      }
+      const float2 p = upk2(P), q = upk2(Q);
+      row[base + w * step] = CT{p.x - q.y, p.y + q.x};
+    }
+  } else {
+#pragma unroll
+    for (int w = 0; w < S; ++w) {
+      CT a = czero<CT>();
+#pragma unroll
+      for (int u = 0; u < S; ++u) cfma(a, Ms[w * S + u], x[u]);
+      row[base + w * step] = a;
+    }
   }
 }
 template <typename CT, int S, int SMAX>

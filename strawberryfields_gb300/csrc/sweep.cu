@@ -182,12 +182,12 @@ __global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)
 // ---------------------------------------------------------------------------
 static int adj_tile(int dtype) { return dtype == FOCK_C64 ? 256 : 128; }
 
-static size_t fwd_smem(int dtype, int D) { return (size_t)D * (D + 1) * (dtype == FOCK_C64 ? 8 : 16); }
+static size_t fwd_smem(int dtype, int D) { return ms_slots(dtype, D) * (dtype == FOCK_C64 ? 8 : 16); }
 
 static size_t bwd_smem(int dtype, int D) {
   const int esz = dtype == FOCK_C64 ? 8 : 16;
   const int rows = 4 * ((D + 3) / 4);
-  return (size_t)esz * ((size_t)((D * (D + 1) + 1) & ~1) + 2 * (size_t)rows * (adj_tile(dtype) + 1));
+  return (size_t)esz * (((ms_slots(dtype, D) + 1) & ~(size_t)1) + 2 * (size_t)rows * (adj_tile(dtype) + 1));
 }
 
 template <typename K>
