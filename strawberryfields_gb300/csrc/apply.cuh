@@ -289,7 +289,7 @@ struct PlaneGeom {
   int two, c_inner;       // two-mode plane; copy with lanes over columns
   int flat;               // plane of column j starts at j*E (gate on the innermost axes)
   unsigned emagic;        // ceil(2^26 / E): idx / E as a multiply-shift
-  int nblk, nrows, G;     // blocks, C rows (sum of sizes), column groups of the C pass
+  int nblk, G, nslot;     // blocks; column groups and (entry, group) slots of the C pass
   int nent, ms_total;     // C entries (= staged matrix entries)
   int sm_goff, sm_cb, sm_tile, smem;  // shared-memory layout (bytes)
   short base[PL_MAX_BLK], step[PL_MAX_BLK], s[PL_MAX_BLK];  // block y: elements base + u*step
@@ -297,7 +297,6 @@ struct PlaneGeom {
   int moff[PL_MAX_BLK];        // stored matrix offset of block y
   int cout_off[PL_MAX_BLK];    // offset of block y's C entries (stored orientation)
   unsigned char rev[PL_MAX_BLK];
-  unsigned char rows_y[PL_THREADS], rows_u[PL_THREADS];  // C row -> (block, position)
   short warp_start[PL_WARPS + 1];
   unsigned short items[PL_MAX_ITEMS];  // (block << 4) | column group, per warp
 };

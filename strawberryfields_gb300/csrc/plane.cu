@@ -19,12 +19,17 @@
 // per (block, column tile), and the next tile's copies are in flight while
 // the current one is computed (two buffers in the apply kernel).
 //
-// The adjoint kernel holds lam_out and psi_in tiles; its C accumulation maps
-// lanes to block rows (thread (b, u) accumulates C_b[u][.] over the tile's
-// columns in registers, psi values broadcast across the rows of a block),
-// then lam_in = M^dagger lam_out is formed in place with the apply mapping
-// and written back.  Per-CTA partial sums of C go to cpart[CTA][entries]
-// (FP64, stored orientation) for a fixed-order reduction.
+// The adjoint kernel holds lam_out and psi_in tiles.  Its C accumulation
+// deals the C entries (block y, row u, column w) out to the threads in equal
+// shares -- thread t owns entries t, t + 256, ... and sums
+// conj(lam[u]) psi[w] over the tile's columns in registers (or over one of G
+// column groups when there are fewer entries than threads), so no thread waits
+// at the barrier for the large blocks' rows; consecutive threads hold
+// consecutive w of one row, so the lam value is a broadcast and the psi values
+// of a half-warp fall in distinct banks.  Then lam_in = M^dagger lam_out is
+// formed in place with the apply mapping and written back.  Per-CTA partial
+// sums of C go to cpart[CTA][entries] (FP64, stored orientation) for a
+// fixed-order reduction.
 //
 // The block structure is the reference's selection rules
 // (strawberryfields/backends/fockbackend/circuit.py:219-365): sum blocks for
@@ -50,6 +55,15 @@ __device__ __forceinline__ void pl_cp(double2* dst, const double2* src) {
 __device__ __forceinline__ void pl_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int N>
 __device__ __forceinline__ void pl_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// C entries of the largest plane with blocks up to SMAX: the sum or
+// difference blocks of a two-mode op (sizes 1..D..1, D(2D^2+1)/3 entries) up
+// to PL_MAX_D2, one dense block of a one-mode op beyond; and the C slots per
+// thread of the adjoint that covers them
+__host__ __device__ constexpr int pl_nent_max(int smax) {
+  return smax <= PL_MAX_D2 ? smax * (2 * smax * smax + 1) / 3 : smax * smax;
+}
+__host__ __device__ constexpr int pl_kmax(int smax) { return (pl_nent_max(smax) + PL_THREADS - 1) / PL_THREADS; }
 
 // columns of a tile that starts at column j0 (the last tile may be partial)
 __device__ __forceinline__ int pl_cols(int64_t tc, int64_t rest) { return (int)(rest < tc ? rest : tc); }
@@ -299,17 +313,30 @@ __global__ void __launch_bounds__(PL_THREADS, 2)
   }
   if (lam_in) pl_stage(MsH, mat, g, mflags | MF_ADJOINT);
 
-  // C rows: thread -> (row r, column group cg); rows sorted by block size
+  // C slots of this thread: slot i = tid + k * PL_THREADS is entry i % nent
+  // summed over the columns col = i / nent (mod G)
+  constexpr int KMAX = pl_kmax(SMAX);
   const int G = g.G;
-  const bool activeA = tid < g.nrows * G;
-  const int r = activeA ? tid % g.nrows : 0;
-  const int cg = tid / g.nrows;
-  const int y = g.rows_y[r], u = g.rows_u[r];
-  const int s = g.s[y], base = g.base[y], step = g.step[y];
-  const int smax_warp = __reduce_max_sync(0xffffffffu, activeA ? s : 0);
-  CT acc[SMAX];
+  short loff[KMAX], poff[KMAX], grp[KMAX];
+  int cout[KMAX];
+  CT acc[KMAX];
 #pragma unroll
-  for (int w = 0; w < SMAX; ++w) acc[w] = czero<CT>();
+  for (int k = 0; k < KMAX; ++k) {
+    acc[k] = czero<CT>();
+    const int i = tid + k * PL_THREADS;
+    grp[k] = -1;
+    if (i < g.nslot) {
+      const int e = i % g.nent;
+      int y = 0;
+      while (y + 1 < g.nblk && e >= g.ms_off[y + 1]) ++y;
+      const int s = g.s[y], r = e - g.ms_off[y], u = r / s, w = r - u * s;
+      loff[k] = (short)(g.base[y] + u * g.step[y]);
+      poff[k] = (short)(g.base[y] + w * g.step[y]);
+      const int a = g.rev[y] ? s - 1 - u : u, b = g.rev[y] ? s - 1 - w : w;
+      cout[k] = g.cout_off[y] + a * s + b;
+      grp[k] = (short)(i / g.nent);
+    }
+  }
 
   // bases of tile t at cb0 + cur*TC, of tile t + GX at the other half
   int cur = 0;
@@ -320,17 +347,12 @@ __global__ void __launch_bounds__(PL_THREADS, 2)
     int64_t* cbn = cb0 + (cur ^ 1) * g.TC;
     pl_wait<0>();
     __syncthreads();
-    if (activeA) {
-      for (int col = cg; col < tcv; col += G) {
-        const CT* lr = L + col * g.EP + base;
-        const CT* pr = P + col * g.EP + base;
-        const CT l = lr[u * step];
 #pragma unroll
-        for (int w = 0; w < SMAX; ++w) {
-          if (w >= smax_warp) break;
-          if (w < s) cfma_conj(acc[w], l, pr[w * step]);
-        }
-      }
+    for (int k = 0; k < KMAX; ++k) {
+      if (grp[k] < 0) break;
+      const CT* lr = L + loff[k];
+      const CT* pr = P + poff[k];
+      for (int col = grp[k]; col < tcv; col += G) cfma_conj(acc[k], lr[col * g.EP], pr[col * g.EP]);
     }
     __syncthreads();
     const int tcn = tn < g.ntiles ? pl_cols(g.TC, g.ncols - tn * g.TC) : 0;
@@ -349,35 +371,26 @@ __global__ void __launch_bounds__(PL_THREADS, 2)
   __syncthreads();
   // partial C of this CTA (stored orientation)
   if (G == 1) {
-    if (activeA) {
-      const int rv = g.rev[y];
-      const int a = rv ? s - 1 - u : u;
-      double2* dst = cpart + g.cout_off[y] + a * s;
 #pragma unroll
-      for (int w = 0; w < SMAX; ++w)
-        if (w < s) dst[rv ? s - 1 - w : w] = to_d(acc[w]);
-    }
+    for (int k = 0; k < KMAX; ++k)
+      if (grp[k] >= 0) cpart[cout[k]] = to_d(acc[k]);
   } else {
-    // sum the G column groups of each row through shared memory (fixed order)
+    // sum the G column groups of each entry through shared memory (fixed order)
     CT* red = L;
-    if (activeA) {
 #pragma unroll
-      for (int w = 0; w < SMAX; ++w)
-        if (w < s) red[((int64_t)cg * g.nrows + r) * g.D + w] = acc[w];
-    }
+    for (int k = 0; k < KMAX; ++k)
+      if (grp[k] >= 0) red[tid + k * PL_THREADS] = acc[k];
     __syncthreads();
-    for (int rr = tid; rr < g.nrows; rr += PL_THREADS) {
-      const int yy = g.rows_y[rr], uu = g.rows_u[rr], ss = g.s[yy], rv = g.rev[yy];
-      const int a = rv ? ss - 1 - uu : uu;
-      for (int w = 0; w < ss; ++w) {
-        double2 sum = make_double2(0.0, 0.0);
-        for (int q = 0; q < G; ++q) {
-          const double2 v = to_d(red[((int64_t)q * g.nrows + rr) * g.D + w]);
-          sum.x += v.x;
-          sum.y += v.y;
-        }
-        cpart[g.cout_off[yy] + a * ss + (rv ? ss - 1 - w : w)] = sum;
+    // G > 1 only when nent <= PL_THREADS / 2: entry tid's group-0 slot is
+    // this thread's slot 0
+    if (tid < g.nent) {
+      double2 sum = make_double2(0.0, 0.0);
+      for (int q = 0; q < G; ++q) {
+        const double2 v = to_d(red[q * g.nent + tid]);
+        sum.x += v.x;
+        sum.y += v.y;
       }
+      cpart[cout[0]] = sum;
     }
   }
 }
@@ -403,7 +416,7 @@ int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, i
   g.flat = v.C == 1 && (!g.two || v.B == 1) ? 1 : 0;
   g.emagic = (unsigned)(((1ull << 26) + g.E - 1) / g.E);
   g.nblk = g.two ? 2 * D - 1 : 1;
-  int ms = 0, rows = 0;
+  int ms = 0;
   for (int y = 0; y < g.nblk; ++y) {
     if (!g.two) {
       g.base[y] = 0; g.step[y] = 1; g.s[y] = (short)D; g.moff[y] = 0; g.rev[y] = 0; g.cout_off[y] = 0;
@@ -431,18 +444,14 @@ int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, i
     }
     g.ms_off[y] = ms;
     ms += g.s[y] * g.s[y];
-    for (int u = 0; u < g.s[y]; ++u) {
-      if (rows >= PL_THREADS) return 0;
-      g.rows_y[rows] = (unsigned char)y;
-      g.rows_u[rows] = (unsigned char)u;
-      ++rows;
-    }
   }
   g.ms_off[g.nblk] = ms;
   g.ms_total = ms;
   g.nent = ms;
-  g.nrows = rows;
-  g.G = std::max(1, PL_THREADS / rows);
+  // C pass: one slot per entry, times G column groups when entries are few
+  g.G = std::max(1, PL_THREADS / ms);
+  g.nslot = ms * g.G;
+  if (g.nslot > PL_THREADS * pl_kmax(D)) return 0;
   // columns per tile: one warp of columns per block for two modes; enough
   // column groups to give every warp a dense block otherwise
   g.TC = g.two ? 32 : 256;
@@ -477,7 +486,7 @@ int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, i
   g.sm_cb = (int)align16((size_t)g.sm_goff + (size_t)g.E * 8);
   g.sm_tile = (int)align16((size_t)g.sm_cb + (size_t)2 * g.TC * 8);
   size_t tiles = (size_t)2 * g.TC * g.EP * esz;
-  if (adjoint) tiles = std::max(tiles, (size_t)PL_THREADS * D * esz);  // column-group reduction
+  if (adjoint) tiles = std::max(tiles, (size_t)g.nslot * esz);  // column-group reduction
   g.smem = (int)(g.sm_tile + tiles);
   if (g.smem > 200 * 1024) return 0;
   *out = g;

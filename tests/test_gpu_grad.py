@@ -307,3 +307,41 @@ def test_tuned_kernels_give_the_same_gradient(cuda):
     g = c.backward(p, s, g_state)[0]
     assert torch.allclose(s, ref_s, rtol=0, atol=1e-13)
     assert torch.allclose(g, ref_g, rtol=1e-11, atol=1e-13)
+
+
+@pytest.mark.parametrize("D", [3, 4, 7, 12, 16, 20])
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_plane_kernels_on_every_op_match_oracle(cuda, D, dtype):
+    """Every op that has a plane-tile kernel switched to it (inner and last
+    axes, one- and two-mode, cutoffs up to the plane limits 16 / 24; small
+    cutoffs exercise the column-group split of the adjoint's C pass) against
+    the oracle's tape adjoint."""
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+    from strawberryfields_gb300.qnn import qnn_gates, qnn_params
+
+    N = 3
+    gates, npar = qnn_gates(N, 1)
+    params = qnn_params(gates, npar, seed=D)
+    tdt = getattr(torch, dtype)
+    circ = CompiledCircuit(N, D, gates, npar, dtype=tdt)
+    n_plane = 0
+    for k in range(circ.n_ops):
+        if circ.op_config(k)[2]:
+            circ.tune_op(k, 1, 0)
+            n_plane += 1
+    assert n_plane > 0
+    rng = np.random.default_rng(D)
+    t = rng.normal(size=(D,) * N) + 1j * rng.normal(size=(D,) * N)
+    t /= np.linalg.norm(t)
+    p = torch.tensor(params, device="cuda", dtype=torch.float64, requires_grad=True)
+    psi = circ(p)
+    tt = torch.as_tensor(t, device="cuda").to(tdt)
+    (1 - torch.abs(torch.sum(tt.conj() * psi)) ** 2).backward()
+    ref_states = fo.run_gates(gates, params, N, D)
+    s = np.vdot(t, ref_states[-1])
+    ref = fo.adjoint_grads(gates, params, N, D, -2 * s * t)
+    tol_s, tol_g = (1e-12, 1e-10) if dtype == "complex128" else (1e-5, 1e-5)
+    assert np.abs(psi.detach().to(torch.complex128).cpu().numpy() - ref_states[-1]).max() < tol_s
+    got = p.grad.cpu().numpy()
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < tol_g
