@@ -422,9 +422,10 @@ def gpu_arm(args, rank, world, cpu_base):
     e2e = {"value": world * 1e3 / e2e_ms, "unit": "grads/s", "h2d_bytes_per_step": npar * 8,
            "d2h_bytes_per_step": npar * 8 + 4, "ms_per_step": e2e_ms}
 
-    # ours per step: matrix build + nops applies (forward); matrix build +
-    # nops adjoints + nops partial-sum reductions + parameter gradients
-    launches = 3 * nops + 3
+    # ours per step (as the ncu launch list shows): one matrix build (the
+    # adjoint sweep reuses the forward sweep's matrices), nops applies, nops
+    # adjoints, one reduction of every op's partial sums, parameter gradients
+    launches = 2 * nops + 3
     out = {
         "metric": "CV-QNN grads/s (batched adjoint vs plain kernel+FD, <=1e-5 err); HBM % of peak",
         "value": round(value, 3), "unit": "grads/s", "n_gpus": world, "steps": args.steps,
