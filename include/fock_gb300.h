@@ -102,6 +102,24 @@ int fock_apply_gate(int kind, double p0, double p1, int mode1, int mode2,
  * to one mode (e.g. cubic phase, fockbackend/circuit.py:590). */
 int fock_apply_matrix1(const void* mat, int mode, int num_modes, int cutoff, int pure, int dtype,
                        const void* in, void* out, void* tmp, void* stream);
+/* Fock matrix of an m-mode Gaussian unitary (m = 1..3) from its Choi
+ * parameters -- the TF backend's Ggate (strawberryfields/backends/tfbackend/
+ * ops.py:457-572: choi_trick, then the renormalised multidimensional Hermite
+ * polynomials of the third-party thewalrus).  R: 2m x 2m complex, y: 2m
+ * complex, C: one complex, all host arrays of (re, im) doubles; mat: device
+ * complex128 [D]^(2m) in C order over (out_1..out_m, in_1..in_m), i.e. the
+ * D^m x D^m matrix from input to output multi-index.  FP64. */
+int fock_gaussian_gate_matrix(int num_gate_modes, int cutoff, const double* R, const double* y,
+                              const double* C, void* mat, void* stream);
+/* Apply a dense D^k x D^k matrix (device complex128, rows the output
+ * multi-index over modes[0..k-1] in C order) to k modes (any order, any
+ * positions): n_mode_gate of tfbackend/ops.py.  Mixed states: M on the ket
+ * axes, conj(M) on the bra axes (tmp: a state-sized buffer).  workspace:
+ * fock_apply_modes_workspace_bytes(k, cutoff, dtype); at most 4096
+ * amplitudes per column (D^k). */
+int64_t fock_apply_modes_workspace_bytes(int k, int cutoff, int dtype);
+int fock_apply_modes(int num_modes, int cutoff, int pure, int dtype, int k, const int* modes, const void* mat,
+                     const void* in, void* out, void* tmp, void* workspace, void* stream);
 /* Diagonal phases: multiply every amplitude by
  * exp(i (sum_m angles[m*D + n_m] + sum_k ck_kappa[k] n_{a_k} n_{b_k}))
  * (bra side conjugated for mixed states).  `angles` device (num_modes*D) or

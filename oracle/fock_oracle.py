@@ -570,6 +570,82 @@ def wigner(rho, xvec, pvec, hbar=2.0):
     return W / hbar
 
 
+def _choi(S, d):
+    """choi_trick of tfbackend/ops.py:457-525: S on m modes of a Choi state
+    (two-mode squeezing arcsinh 1 per mode), Husimi covariance -> Hermite
+    matrix, R from its 2m x 2m corner rescaled by 1/tanh(arcsinh 1)
+    on the reference half, y and C from alpha = (d_x + i d_p) / 2."""
+    S = np.asarray(S, dtype=CDT)
+    d = np.asarray(d, dtype=CDT)
+    m = S.shape[0] // 2
+    alpha = (d[:m] + 1j * d[m:]) / 2
+    r = np.arcsinh(1.0)
+    O, Id = np.zeros((m, m)), np.eye(m)
+    choi_s = np.block([[np.cosh(r) * Id, np.sinh(r) * Id, O, O], [np.sinh(r) * Id, np.cosh(r) * Id, O, O],
+                       [O, O, np.cosh(r) * Id, -np.sinh(r) * Id], [O, O, -np.sinh(r) * Id, np.cosh(r) * Id]])
+    full = np.block([[S[:m, :m], O, S[:m, m:], O], [O, Id, O, O], [S[m:, :m], O, S[m:, m:], O], [O, O, O, Id]])
+    Sx = full @ choi_s
+    V = 0.5 * Sx @ Sx.T
+    I2 = np.eye(2 * m)
+    T = np.sqrt(0.5) * np.block([[I2, 1j * I2], [I2, -1j * I2]])
+    sq = T @ V @ T.conj().T + 0.5 * np.eye(4 * m)
+    X = np.block([[np.zeros((2 * m, 2 * m)), I2], [I2, np.zeros((2 * m, 2 * m))]])
+    A = X @ (np.eye(4 * m) - np.linalg.inv(sq))
+    E = np.diag(np.r_[np.ones(m), np.ones(m) / np.tanh(r)])
+    R = -np.conj(E @ A[:2 * m, :2 * m] @ E)
+    y = np.r_[R[:m, :m] @ alpha.conj() + alpha, R[m:, :m] @ alpha.conj()]
+    at = np.r_[alpha, np.zeros(m)]
+    C = np.sqrt(np.sqrt(np.linalg.det(np.eye(m) - R[:m, :m] @ R[:m, :m].conj()) + 0j)) * np.exp(
+        -0.5 * np.sum(at.conj() * (at + R @ at.conj())))
+    return R, y, C
+
+
+def gaussian_gate_matrix(S, d, D):
+    """Fock matrix of the m-mode Gaussian unitary with symplectic S (xxpp)
+    and displacement d, as the reference's TF backend forms it
+    (strawberryfields/backends/tfbackend/ops.py:457-572): choi_trick's
+    (R, y, C), then the renormalised multidimensional Hermite tensor of the
+    third-party thewalrus (not vendored; restated from its recurrence
+    G[k] = (y_i G[k-e_i] - sum_j R_ij sqrt(k_j - d_ij) G[k-e_i-e_j]) / sqrt(k_i),
+    i the first nonzero index, G[0] = C).  Returns [out_1..out_m, in_1..in_m].
+    Pinned by tests/test_oracle.py against the exact truncated matrices of
+    the squeezer, displacement, rotation, beamsplitter and two-mode squeezer."""
+    import itertools
+
+    R, y, C = _choi(S, d)
+    n = len(y)
+    G = np.zeros((D,) * n, dtype=CDT)
+    for k in itertools.product(range(D), repeat=n):
+        if not any(k):
+            G[k] = C
+            continue
+        i = next(j for j in range(n) if k[j] > 0)
+        km = list(k)
+        km[i] -= 1
+        v = y[i] * G[tuple(km)]
+        for j in range(n):
+            if km[j] > 0:
+                kk = list(km)
+                kk[j] -= 1
+                v -= R[i, j] * math.sqrt(km[j]) * G[tuple(kk)]
+        G[k] = v / math.sqrt(k[i])
+    return G
+
+
+def apply_gate_modes(state, G, modes, pure=True):
+    """Apply G [out_1..out_k, in_1..in_k] to ``modes`` of a ket, or as
+    G rho G^dagger to a density matrix (interleaved axes)."""
+    k = len(modes)
+    axes_k = list(modes) if pure else [2 * m for m in modes]
+    out = np.tensordot(G, state, axes=(list(range(k, 2 * k)), axes_k))
+    out = np.moveaxis(out, list(range(k)), axes_k)
+    if pure:
+        return out
+    axes_b = [2 * m + 1 for m in modes]
+    out = np.tensordot(G.conj(), out, axes=(list(range(k, 2 * k)), axes_b))
+    return np.moveaxis(out, list(range(k)), axes_b)
+
+
 def homodyne_project(state, phi, x, mode, n, pure=True, hbar=2.0):
     """State after a homodyne outcome ``x`` on ``mode`` (reference
     circuit.py:766-795): |0><x_phi| applied to the mode, with x_phi =

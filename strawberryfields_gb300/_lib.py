@@ -64,6 +64,9 @@ _SIGS = {
     "fock_expand_blocks": (_i, [_i, _i, _vp, _vp, _vp]),
     "fock_apply_gate": (_i, [_i, _d, _d, _i, _i, _i, _i, _i, _i, _dp, _vp, _vp, _vp, _vp, _vp]),
     "fock_apply_matrix1": (_i, [_vp, _i, _i, _i, _i, _i, _vp, _vp, _vp, _vp]),
+    "fock_gaussian_gate_matrix": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp]),
+    "fock_apply_modes_workspace_bytes": (ctypes.c_int64, [_i, _i, _i]),
+    "fock_apply_modes": (_i, [_i, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fock_apply_phases": (_i, [_i, _i, _i, _i, _vp, _i, _ip, _dp, _vp, _vp, _vp]),
     "fock_mix": (_i, [_i, _i, _i, _vp, _vp, _vp]),
     "fock_vacuum": (_i, [_i, _i, _i, _i, _vp, _vp]),

@@ -206,6 +206,11 @@ class FockGB300Backend:
     def loss(self, T, mode):
         self.circuit.loss(T, self._remap_modes(mode))
 
+    def gaussian_gate(self, S, d, *modes):
+        """N-mode Gaussian gate (the TF backend's gaussian_gate,
+        tfbackend/backend.py:231); S symplectic (xxpp), d displacements."""
+        self.circuit.gaussian_gate(S, d, self._remap_modes(list(modes)))
+
     # ----------------------------------------------------------------- measurement
     def measure_fock(self, modes, shots=1, select=None, **kwargs):
         if shots != 1:

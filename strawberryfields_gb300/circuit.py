@@ -9,6 +9,7 @@ that mode (``pre`` phases of ``fock_apply_gate``), or flushed as one diagonal
 pass before any readout -- the state crosses HBM once per gate group.
 """
 
+import ctypes
 import math
 import numbers
 
@@ -201,6 +202,44 @@ class DeviceCircuit:
         L.call("fock_apply_matrix1", mat_dev.data_ptr(), mode, self._num_modes, self._trunc, int(self._pure),
                self._dcode, self._state.data_ptr(), out.data_ptr(),
                tmp.data_ptr() if tmp is not None else None, self._stream())
+        self._state = out
+
+    def gaussian_gate(self, S, d, modes):
+        """General Gaussian unitary with symplectic S (xxpp) and displacement d
+        on ``modes`` (the TF backend's Ggate, tfbackend/circuit.py:565 and
+        ops.py:457-572, 1115): Choi parameters on the host, the D^m x D^m Fock
+        matrix by the Hermite recurrence on the device (FP64), one dense
+        k-mode pass (ket and bra passes for a density matrix)."""
+        from . import gaussian
+
+        modes = [int(m) for m in modes]
+        S = np.asarray(S)
+        d = np.asarray(d)
+        gaussian.check_gate(S, d)
+        m = len(modes)
+        if S.shape[0] != 2 * m:
+            raise ValueError("The matrix S must act on the given modes (2 x number of modes rows).")
+        if len(set(modes)) != m:
+            raise ValueError("The specified modes cannot be duplicated.")
+        self._flush(modes)
+        R, y, C = gaussian.choi_parameters(S, d)
+        D = self._trunc
+        mat = torch.empty([D] * (2 * m), dtype=torch.complex128, device=self._device)
+        Rh = np.ascontiguousarray(R, dtype=np.complex128).view(np.float64)
+        yh = np.ascontiguousarray(y, dtype=np.complex128).view(np.float64)
+        Ch = np.array([C.real, C.imag], dtype=np.float64)
+        lib = L.load()
+        L.check(lib.fock_gaussian_gate_matrix(m, D, Rh.ctypes.data, yh.ctypes.data, Ch.ctypes.data,
+                                              mat.data_ptr(), self._stream()), "fock_gaussian_gate_matrix")
+        ws = torch.empty(int(lib.fock_apply_modes_workspace_bytes(m, D, self._dcode)), dtype=torch.uint8,
+                         device=self._device)
+        out = self._empty()
+        tmp = None if self._pure else self._empty()
+        md = (ctypes.c_int * m)(*modes)
+        L.check(lib.fock_apply_modes(self._num_modes, D, int(self._pure), self._dcode, m, md, mat.data_ptr(),
+                                     self._state.data_ptr(), out.data_ptr(),
+                                     tmp.data_ptr() if tmp is not None else None, ws.data_ptr(), self._stream()),
+                "fock_apply_modes")
         self._state = out
 
     def cubic_phase_shift(self, gamma, mode):

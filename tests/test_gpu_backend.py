@@ -302,3 +302,75 @@ def test_homodyne_coherent_state_moments(cuda):
     var = np.sum(q * q * p) / np.sum(p) - mean ** 2
     assert abs(mean - 2 * 0.7 * np.cos(0.3)) < 1e-6
     assert abs(var - 1.0) < 1e-6
+
+
+def _random_symplectic(m, seed):
+    """A product of single-mode squeezers and rotations and beamsplitters
+    (xxpp ordering)."""
+    rng = np.random.default_rng(seed)
+
+    def embed(Sk, modes):
+        S = np.eye(2 * m)
+        idx = list(modes) + [m + j for j in modes]
+        S[np.ix_(idx, idx)] = Sk
+        return S
+
+    S = np.eye(2 * m)
+    for j in range(m):
+        r, ph, t = rng.uniform(0.1, 0.4), rng.uniform(0, 6), rng.uniform(0, 6)
+        c, s = np.cosh(r), np.sinh(r)
+        sq = np.array([[c - np.cos(ph) * s, -np.sin(ph) * s], [-np.sin(ph) * s, c + np.cos(ph) * s]])
+        rt = np.array([[np.cos(t), -np.sin(t)], [np.sin(t), np.cos(t)]])
+        S = embed(rt @ sq, [j]) @ S
+    for j in range(m - 1):
+        th, ph = rng.uniform(0, 1.5), rng.uniform(0, 6)
+        ct, st, cp, sp = np.cos(th), np.sin(th), np.cos(ph), np.sin(ph)
+        B = np.array([[ct, -cp * st, 0, -st * sp], [cp * st, ct, -st * sp, 0],
+                      [0, st * sp, ct, -cp * st], [st * sp, 0, cp * st, ct]])
+        S = embed(B, [j, j + 1]) @ S
+    return S, rng.uniform(-0.4, 0.4, 2 * m)
+
+
+@pytest.mark.parametrize("m,D", [(1, 9), (2, 6), (3, 4)])
+def test_gaussian_gate_matrix_on_device(cuda, m, D):
+    """The device Hermite recurrence against the oracle's (FP64, 1e-12)."""
+    import ctypes
+
+    import torch
+    from strawberryfields_gb300 import _lib as L
+    from strawberryfields_gb300 import gaussian
+
+    S, d = _random_symplectic(m, 10 + m)
+    R, y, C = gaussian.choi_parameters(S, d)
+    mat = torch.empty([D] * (2 * m), dtype=torch.complex128, device="cuda")
+    Rh = np.ascontiguousarray(R).view(np.float64)
+    yh = np.ascontiguousarray(y).view(np.float64)
+    Ch = np.array([C.real, C.imag])
+    L.check(L.load().fock_gaussian_gate_matrix(m, D, Rh.ctypes.data, yh.ctypes.data, Ch.ctypes.data,
+                                               mat.data_ptr(), None), "fock_gaussian_gate_matrix")
+    ref = fo.gaussian_gate_matrix(S, d, D)
+    assert np.abs(mat.cpu().numpy() - ref).max() < 1e-12
+    assert ctypes is not None
+
+
+@pytest.mark.parametrize("pure", [True, False])
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_gaussian_gate_on_states(cuda, pure, dtype):
+    """Ggate on modes (2, 0) of a 3-mode state after a few gates, against the
+    oracle's dense apply (ket, or G rho G^dagger)."""
+    D = 6
+    b = make_backend(3, D, pure, dtype)
+    b.squeeze(0.2, 0.3, 0)
+    b.displacement(0.3, 1.0, 1)
+    b.beamsplitter(0.5, 0.2, 0, 2)
+    s0 = b.state()
+    before = s0.ket() if pure else s0.dm()
+    S, d = _random_symplectic(2, 3)
+    b.gaussian_gate(S, d, 2, 0)
+    got = b.state().ket() if pure else b.state().dm()
+    G = fo.gaussian_gate_matrix(S, d, D)
+    ref = fo.apply_gate_modes(before.astype(np.complex128), G, [2, 0], pure)
+    tol = 1e-12 if dtype == "complex128" else 1e-5
+    assert np.abs(got - ref).max() < tol
+    with pytest.raises(ValueError, match="not symplectic"):
+        b.gaussian_gate(S * 1.2, d, 2, 0)

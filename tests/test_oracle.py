@@ -299,3 +299,62 @@ def test_poly_quad_expectation_argument_checks():
     with pytest.raises(ValueError, match="length 2N"):
         h.s.poly_quad_expectation(np.eye(4), np.ones(3))
     assert h.s.poly_quad_expectation(None, None, 2.5) == (2.5, 0.0)
+
+
+def _symplectics():
+    """thewalrus-convention symplectic matrices (xxpp) of the SF gates."""
+    def sq(r, phi):
+        c, s = np.cosh(r), np.sinh(r)
+        return np.array([[c - np.cos(phi) * s, -np.sin(phi) * s], [-np.sin(phi) * s, c + np.cos(phi) * s]])
+
+    def rot(t):
+        return np.array([[np.cos(t), -np.sin(t)], [np.sin(t), np.cos(t)]])
+
+    def bs(th, ph):
+        ct, st, cp, sp = np.cos(th), np.sin(th), np.cos(ph), np.sin(ph)
+        return np.array([[ct, -cp * st, 0, -st * sp], [cp * st, ct, -st * sp, 0],
+                         [0, st * sp, ct, -cp * st], [st * sp, 0, cp * st, ct]])
+
+    def s2(r, ph):
+        ch, sh, cp, sp = np.cosh(r), np.sinh(r), np.cos(ph), np.sin(ph)
+        return np.array([[ch, cp * sh, 0, sp * sh], [cp * sh, ch, sp * sh, 0],
+                         [0, sp * sh, ch, -cp * sh], [sp * sh, 0, -cp * sh, ch]])
+
+    return sq, rot, bs, s2
+
+
+def test_gaussian_gate_matrix_is_the_exact_gate():
+    """The Ggate restatement (choi_trick + renormalised Hermite recurrence)
+    reproduces the exact truncated matrices of the squeezer, displacement,
+    rotation, beamsplitter and two-mode squeezer (themselves pinned to expm):
+    this fixes its conventions (xxpp symplectic, d = (x, p) with hbar 2,
+    output indices first)."""
+    sq, rot, bs, s2 = _symplectics()
+    D = 7
+    G = fo.gaussian_gate_matrix(sq(0.4, 0.7), np.zeros(2), D)
+    assert np.abs(G - fo.squeezing(0.4, 0.7, D)).max() < 1e-13
+    al = 0.3 * np.exp(0.5j)
+    G = fo.gaussian_gate_matrix(np.eye(2), [2 * al.real, 2 * al.imag], D)
+    assert np.abs(G - fo.displacement(0.3, 0.5, D)).max() < 1e-13
+    assert np.abs(fo.gaussian_gate_matrix(rot(0.6), np.zeros(2), D) - fo.phase(0.6, D)).max() < 1e-13
+    D = 6
+    G = fo.gaussian_gate_matrix(bs(0.7, 0.4), np.zeros(4), D)
+    assert np.abs(G.transpose(0, 2, 1, 3) - fo.beamsplitter(0.7, 0.4, D)).max() < 1e-13
+    G = fo.gaussian_gate_matrix(s2(0.3, 1.1), np.zeros(4), D)
+    assert np.abs(G.transpose(0, 2, 1, 3) - fo.two_mode_squeeze(0.3, 1.1, D)).max() < 1e-13
+
+
+def test_gaussian_host_choi_matches_oracle():
+    from strawberryfields_gb300 import gaussian
+
+    sq, rot, bs, s2 = _symplectics()
+    S = bs(0.3, 0.9) @ np.kron(np.eye(2), np.eye(2))
+    d = np.array([0.2, -0.1, 0.3, 0.05])
+    R1, y1, C1 = gaussian.choi_parameters(S, d)
+    R2, y2, C2 = fo._choi(S, d)
+    assert np.abs(R1 - R2).max() < 1e-14 and np.abs(y1 - y2).max() < 1e-14 and abs(C1 - C2) < 1e-14
+    assert gaussian.is_symplectic(S) and not gaussian.is_symplectic(S * 1.1)
+    with pytest.raises(ValueError, match="not symplectic"):
+        gaussian.check_gate(S * 1.1, d)
+    with pytest.raises(ValueError, match="compatible"):
+        gaussian.check_gate(S, d[:2])
