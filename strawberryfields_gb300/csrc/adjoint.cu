@@ -51,11 +51,11 @@ __global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)
   const int bs = layout == LAYOUT_DENSE ? 0 : ((layout == LAYOUT_DIFF && (mflags & MF_SWAP)) ? 2 * D - 2 - b : b);
   double2* mypart = cpart + sc.part_off[bs] + (int64_t)xrank * s * s;
   CT* MsH = reinterpret_cast<CT*>(smem_raw);
-  CT* lam_s = MsH + ((s * ms_stride<CT>(s) + 1) & ~1);
+  CT* lam_s = MsH + ((ms_slots(sizeof(CT) == 8 ? FOCK_C64 : FOCK_C128, D) + 1) & ~(size_t)1);
   CT* psi_s = lam_s + rows * (TILE + 1);
   pdl_wait();
   pdl_launch_dependents();
-  AdjDispatch<CT, 1, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s, g, mypart,
+  AdjDispatch<CT, kSStep, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s, g, mypart,
                                       xrank, gxb, write_lam);
 }
 

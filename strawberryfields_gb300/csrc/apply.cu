@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(APPLY_THREADS, ApplyMinBlocks<DMAX>::value) ap
   const int64_t j0 = (int64_t)blockIdx.x * (APPLY_THREADS * APPLY_COLS) + threadIdx.x;
   pdl_wait();
   pdl_launch_dependents();
-  ApplyDispatch<CT, 1, DMAX>::run(in, out, v, D, Ms, mat, mflags, g, j0);
+  ApplyDispatch<CT, kSStep, DMAX>::run(in, out, v, D, Ms, mat, mflags, g, j0);
 }
 
 template <typename CT, int DMAX>

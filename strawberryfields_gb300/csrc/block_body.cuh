@@ -31,13 +31,31 @@ __device__ __forceinline__ void apply_cols(const CT* __restrict__ in, CT* __rest
                                            const AxisView& v, int D, CT* Ms, const double2* mat, int mflags,
                                            const BlockGeom& g, int64_t j0) {
   const bool valid = j0 < v.ncols;
+  const int s = g.s;  // <= S
   const int64_t b0 = valid ? col_base(v, j0, D) + g.boff : 0;
   CT x0[S];
+  // complex64 column contiguous in memory (a one-mode op on the innermost
+  // axis) with an even length on a 16-byte boundary: 16-byte loads and
+  // stores of element pairs, half the memory instructions
+  const bool pairs = sizeof(CT) == 8 && g.step == 1 && !(s & 1) && !(b0 & 1);
   if (valid) {
+    if constexpr (sizeof(CT) == 8) {
+      if (pairs) {
+        const float4* p4 = reinterpret_cast<const float4*>(in + b0);
 #pragma unroll
-    for (int u = 0; u < S; ++u) x0[u] = ld_state<COH>(in + b0 + u * g.step);
+        for (int u2 = 0; u2 < S / 2; ++u2) {
+          const float4 q = 2 * u2 < s ? ld_state<COH>(p4 + u2) : make_float4(0.f, 0.f, 0.f, 0.f);
+          x0[2 * u2] = CT{q.x, q.y};
+          x0[2 * u2 + 1] = CT{q.z, q.w};
+        }
+      }
+    }
+    if (!pairs) {
+#pragma unroll
+      for (int u = 0; u < S; ++u) x0[u] = u < s ? ld_state<COH>(in + b0 + u * g.step) : czero<CT>();
+    }
   }
-  stage_block(Ms, mat, g, mflags);
+  stage_block_pad<CT, S>(Ms, mat, g, mflags);
   __syncthreads();
   if (!valid) return;
   constexpr int SP = sizeof(CT) == 8 ? (S + 1) & ~1 : S;
@@ -45,8 +63,20 @@ __device__ __forceinline__ void apply_cols(const CT* __restrict__ in, CT* __rest
   xc.set(x0);
   // rows one at a time: unrolled, the loads of later rows run ahead and
   // spill the column's registers
+  if constexpr (sizeof(CT) == 8) {
+    if (pairs) {
 #pragma unroll 1
-  for (int w = 0; w < S; ++w) {
+      for (int w = 0; w < s; w += 2) {
+        CT a0 = czero<CT>(), a1 = czero<CT>();
+        row_mac<S>(a0, Ms + w * SP, xc);
+        row_mac<S>(a1, Ms + (w + 1) * SP, xc);
+        *reinterpret_cast<float4*>(out + b0 + w) = make_float4(a0.x, a0.y, a1.x, a1.y);
+      }
+      return;
+    }
+  }
+#pragma unroll 1
+  for (int w = 0; w < s; ++w) {
     CT a0 = czero<CT>();
     row_mac<S>(a0, Ms + w * SP, xc);
     out[b0 + w * g.step] = a0;
@@ -72,17 +102,17 @@ __device__ void apply_cols_generic(const CT* __restrict__ in, CT* __restrict__ o
   }
 }
 
-// s == S ? run the unrolled body : try S + 1 (up to DMAX)
+// s <= S ? run the unrolled body of size S : try S + kSStep (up to DMAX)
 template <typename CT, int S, int DMAX, bool COH = false>
 struct ApplyDispatch {
   __device__ __forceinline__ static void run(const CT* in, CT* out, const AxisView& v, int D, CT* Ms,
                                              const double2* mat, int mflags, const BlockGeom& g, int64_t j0) {
-    if (g.s == S) apply_cols<CT, S, COH>(in, out, v, D, Ms, mat, mflags, g, j0);
-    else ApplyDispatch<CT, S + 1, DMAX, COH>::run(in, out, v, D, Ms, mat, mflags, g, j0);
+    if (g.s <= S) apply_cols<CT, S, COH>(in, out, v, D, Ms, mat, mflags, g, j0);
+    else ApplyDispatch<CT, S + kSStep, DMAX, COH>::run(in, out, v, D, Ms, mat, mflags, g, j0);
   }
 };
 template <typename CT, int DMAX, bool COH>
-struct ApplyDispatch<CT, DMAX + 1, DMAX, COH> {
+struct ApplyDispatch<CT, DMAX + kSStep, DMAX, COH> {
   __device__ __forceinline__ static void run(const CT* in, CT* out, const AxisView& v, int D, CT* Ms,
                                              const double2* mat, int mflags, const BlockGeom& g, int64_t j0) {
     apply_cols_generic<CT, COH>(in, out, v, D, Ms, mat, mflags, g, j0);
@@ -119,6 +149,7 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
   constexpr int NG = TILE / 16;
   constexpr int LD = TILE + 1;  // padded row stride (elements)
   const int tid = threadIdx.x;
+  const int s = g.s;  // <= S
   const int owner = tid / NG, grp = tid - owner * NG;
   const int ro = owner >> 2, co = owner & 3;
   CT acc[RR][RR];
@@ -136,16 +167,17 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
     tile_base = base;
 #pragma unroll
     for (int u = 0; u < S; ++u) {
-      const int64_t off = valid ? base + u * g.step : 0;
-      cp_async_elem(&lam_s[u * LD + tid], lam_out + off, valid);
-      cp_async_elem(&psi_s[u * LD + tid], psi_in + off, valid);
+      const bool vu = valid && u < s;  // rows s..S-1 zero-filled
+      const int64_t off = vu ? base + u * g.step : 0;
+      cp_async_elem(&lam_s[u * LD + tid], lam_out + off, vu);
+      cp_async_elem(&psi_s[u * LD + tid], psi_in + off, vu);
     }
     cp_async_commit();
   };
   // the first tile's copies are in flight while the block is staged
   if (xrank < ntiles) issue(xrank);
-  if (write_lam) stage_block(MsH, mat, g, mflags | MF_ADJOINT);
-  // padding rows s..4*RR-1 stay zero
+  if (write_lam) stage_block_pad<CT, S>(MsH, mat, g, mflags | MF_ADJOINT);
+  // padding rows S..4*RR-1 stay zero
   for (int e = tid; e < (4 * RR - S) * LD; e += TILE) {
     lam_s[S * LD + e] = czero<CT>();
     psi_s[S * LD + e] = czero<CT>();
@@ -164,7 +196,7 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
       ColRegs<CT, S> lc;
       lc.set(lam);
 #pragma unroll 1
-      for (int w = 0; w < S; ++w) {
+      for (int w = 0; w < s; ++w) {
         CT a = czero<CT>();
         row_mac<S>(a, MsH + w * SP, lc);
         lam_in[base + w * g.step] = a;
@@ -204,10 +236,10 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
 #pragma unroll
       for (int c = 0; c < RR; ++c) {
         int u = ro * RR + r, w = co * RR + c;
-        if (u < S && w < S) {
-          int a = g.rev ? S - 1 - u : u;
-          int b = g.rev ? S - 1 - w : w;
-          mypart[a * S + b] = to_d(acc[r][c]);
+        if (u < s && w < s) {
+          int a = g.rev ? s - 1 - u : u;
+          int b = g.rev ? s - 1 - w : w;
+          mypart[a * s + b] = to_d(acc[r][c]);
         }
       }
   }
@@ -255,16 +287,16 @@ struct AdjDispatch {
                                              int D, CT* MsH, const double2* mat, int mflags, CT* lam_s, CT* psi_s,
                                              const BlockGeom& g, double2* mypart, int xrank, int gxb,
                                              int write_lam) {
-    if (g.s == S)
+    if (g.s <= S)
       adjoint_body<CT, S, TILE>(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s, g, mypart, xrank,
                                 gxb, write_lam);
     else
-      AdjDispatch<CT, S + 1, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s, g,
-                                              mypart, xrank, gxb, write_lam);
+      AdjDispatch<CT, S + kSStep, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s,
+                                                   g, mypart, xrank, gxb, write_lam);
   }
 };
 template <typename CT, int DMAX, int TILE>
-struct AdjDispatch<CT, DMAX + 1, DMAX, TILE> {
+struct AdjDispatch<CT, DMAX + kSStep, DMAX, TILE> {
   __device__ __forceinline__ static void run(const CT* psi_in, const CT* lam_out, CT* lam_in, const AxisView& v,
                                              int D, CT* MsH, const double2* mat, int mflags, CT*, CT*,
                                              const BlockGeom& g, double2* mypart, int xrank, int gxb,

@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(APPLY_THREADS, ApplyMinBlocks<DMAX>::value)
       const int b = layout == LAYOUT_DENSE ? 0 : block_of_y(D, y);
       const BlockGeom g = block_geom(v, D, layout, b, (mflags & MF_SWAP) ? 1 : 0);
       const int64_t j0 = (int64_t)x * APPLY_THREADS + threadIdx.x;
-      ApplyDispatch<CT, 1, DMAX, true>::run(cur, dst, v, D, Ms, mat, mflags, g, j0);
+      ApplyDispatch<CT, kSStep, DMAX, true>::run(cur, dst, v, D, Ms, mat, mflags, g, j0);
       it = next;
       par ^= 1;
     }
@@ -128,9 +128,9 @@ __global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)
           layout == LAYOUT_DENSE ? 0 : ((layout == LAYOUT_DIFF && (mflags & MF_SWAP)) ? 2 * D - 2 - b : b);
       double2* mypart = cpart + op->part_base + sc.part_off[bs] + (int64_t)xrank * s * s;
       CT* MsH = reinterpret_cast<CT*>(smem_raw);
-      CT* lam_s = MsH + ((s * ms_stride<CT>(s) + 1) & ~1);
+      CT* lam_s = MsH + ((ms_slots(sizeof(CT) == 8 ? FOCK_C64 : FOCK_C128, D) + 1) & ~(size_t)1);
       CT* psi_s = lam_s + rows * (TILE + 1);
-      AdjDispatch<CT, 1, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, arena + op->m_off, mflags, lam_s,
+      AdjDispatch<CT, kSStep, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, arena + op->m_off, mflags, lam_s,
                                           psi_s, g, mypart, xrank, gxb, 1);
     }
     if (!sweep_barrier(sync)) return;
