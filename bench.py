@@ -396,6 +396,52 @@ def gpu_arm(args, rank, world, cpu_base):
     fwd_s = e0.elapsed_time(e1) / nrep / 1e3
     fd_grads_per_s = 1.0 / ((2 * npar + 1) * fwd_s)
 
+    def fwd_ms(c, pp, reps=10):
+        for _ in range(3):
+            c.forward_states(pp, store_all=False)
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(reps):
+            c.forward_states(pp, store_all=False)
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    # the forward configurations: the QNN forward in complex128 too, and the
+    # 3-mode cutoff-10 complex128 plain circuit (per mode S and D, BS on
+    # (0,1) and (1,2), R and K per mode; seeded parameters)
+    c128 = CompiledCircuit(N_MODES, CUTOFF, gates, npar, dtype=torch.complex128, device=dev)
+    q128_ms = fwd_ms(c128, p_dev)
+    del c128
+    g3, np3 = [], 0
+    for m in range(3):
+        g3 += [(_lib.SQUEEZE, m, -1, np3), (_lib.DISPLACEMENT, m, -1, np3 + 2)]
+        np3 += 4
+    g3 += [(_lib.BEAMSPLITTER, 0, 1, np3), (_lib.BEAMSPLITTER, 1, 2, np3 + 2)]
+    np3 += 4
+    for m in range(3):
+        g3 += [(_lib.ROTATION, m, -1, np3), (_lib.KERR, m, -1, np3 + 1)]
+        np3 += 2
+    rng3 = np.random.default_rng(0)
+    p3 = torch.tensor(rng3.uniform(0, 0.5, np3), device=dev)
+    c3 = CompiledCircuit(3, 10, g3, np3, dtype=torch.complex128, device=dev)
+    plain3_ms = fwd_ms(c3, p3, 50)
+    del c3
+    S64 = circ.info.state_bytes
+    flops = circ.info.flops_fwd  # real flops of one forward (the apply kernels' MACs)
+    forward_configs = {
+        "qnn6x12_complex64": {"ms": 1e3 * fwd_s, "gates_per_s": len(gates) / fwd_s,
+                              "gbs": 2 * S64 * nops / fwd_s / 1e9, "fp32_tflops": flops / fwd_s / 1e12},
+        "qnn6x12_complex128": {"ms": q128_ms, "gates_per_s": len(gates) / (q128_ms / 1e3),
+                               "gbs": 4 * S64 * nops / (q128_ms / 1e3) / 1e9,
+                               "fp64_tflops": flops / (q128_ms / 1e3) / 1e12,
+                               "fp64_note": "GB300 FP64 is about 1.25 TFLOP/s nominal: the complex128 sweep is "
+                                            "FP64-pipe-bound"},
+        "plain3x10_complex128": {"us": 1e3 * plain3_ms, "gates_per_s": len(g3) / (plain3_ms / 1e3),
+                                 "circuits_per_s": 1e3 / plain3_ms},
+        "note": "forward sweeps only (matrix build included), states L2-resident, no flush between reps",
+    }
+
     # end to end through the public API with host buffers: params H2D,
     # gradient + loss D2H every step
     p_host = torch.tensor(params).pin_memory()
@@ -440,6 +486,7 @@ def gpu_arm(args, rank, world, cpu_base):
         "fd_baseline": {"gpu_forward_ms": 1e3 * fwd_s, "grads_per_s": fd_grads_per_s,
                         "adjoint_speedup": value / world / fd_grads_per_s},
         "batched_throughput": batched,
+        "forward_configs": forward_configs,
         "clocks": clk, "cpu_baseline": cpu_base,
     }
     return out
