@@ -494,7 +494,7 @@ def gpu_arm(args, rank, world, cpu_base):
 
 def single_gate_case(args):
     """Single-gate kernels on a 7-mode cutoff-12 complex64 ket (287 MB, larger
-    than L2): forward apply and adjoint of a squeezer on an inner axis and on
+    than L2; --modes / --cutoff choose another): forward apply and adjoint of a squeezer on an inner axis and on
     the last axis, and of a beamsplitter on an inner and on the last adjacent
     pair.  Each op is its own compiled one-gate circuit, timed with the plan's
     per-op events (apply = the apply launch; adjoint = the adjoint launch and
@@ -509,7 +509,7 @@ def single_gate_case(args):
 
     dev = torch.device("cuda", 0)
     lib = _lib.load()
-    N, D = args.modes, 12
+    N, D = args.modes, args.cutoff
     cases = {"dense1_inner": [(4, 2, -1, 0)], "dense1_last": [(4, N - 1, -1, 0)],
              "block2_inner": [(5, 2, 3, 0)], "block2_last": [(5, N - 2, N - 1, 0)]}
     if args.only:
@@ -719,7 +719,8 @@ def main():
     ap.add_argument("--case", default="gradient", choices=["gradient", "single-gate", "batched", "lossy"])
     ap.add_argument("--circuits", type=int, default=4096)
     ap.add_argument("--only", default="", help="single-gate case: comma-separated subset of the kernels")
-    ap.add_argument("--modes", type=int, default=7, help="single-gate case: modes of the cutoff-12 ket")
+    ap.add_argument("--modes", type=int, default=7, help="single-gate case: modes of the ket")
+    ap.add_argument("--cutoff", type=int, default=12, help="single-gate case: cutoff of the ket")
     ap.add_argument("--eager", action="store_true", help="no CUDA graph capture")
     ap.add_argument("--no-autotune", action="store_true", help="default kernel selection (no per-op tuning)")
     ap.add_argument("--batch", type=int, default=16,
