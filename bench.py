@@ -202,12 +202,14 @@ def _traffic():
 
 def _autotune(circ, p):
     cfgs, ms0, ms1 = circ.autotune(p)
-    ctas = {}
-    for fam, c in cfgs:
+    ctas, tiles = {}, {}
+    for fam, c, tc in cfgs:
         if fam == 0:
             ctas[str(c)] = ctas.get(str(c), 0) + 1
+        else:
+            tiles[str(tc)] = tiles.get(str(tc), 0) + 1
     return {"sweep_ms_before": round(ms0, 4), "sweep_ms_after": round(ms1, 4),
-            "plane_ops": sum(1 for fam, _ in cfgs if fam == 1), "block_ops_by_adjoint_ctas_per_sm": ctas}
+            "plane_ops_by_tile_columns": tiles, "block_ops_by_adjoint_ctas_per_sm": ctas}
 
 
 def gpu_arm(args, rank, world, cpu_base):

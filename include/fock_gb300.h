@@ -259,13 +259,16 @@ int fock_wigner(int cutoff, const void* rho, const double* xvec, int nx, const d
  * keeps the fastest per op).  family: 0 block kernels (one column per
  * thread), 1 plane-tile kernels (two-mode ops whose plane geometry exists:
  * `plane_ok`), -1 unchanged; adj_ctas_per_sm: CTAs per SM of the block
- * adjoint launch (1..64; 0 unchanged; default 8).  Changes the partial-sum
+ * adjoint launch (1..64; 0 unchanged; default 8); plane_tile_columns:
+ * columns per plane tile of a two-mode op (8..32; 0 unchanged; default 32;
+ * op_config reports the dense ops' fixed tile).  Changes the partial-sum
  * layout and so workspace_bytes (read fock_plan_get_info again and
  * reallocate the workspace) and any captured graph of the plan.  Call with no
  * sweep of the plan in flight.  No reference counterpart (the reference has
  * one einsum per gate, tfbackend/ops.py:688-854). */
-int fock_plan_tune(fock_plan* plan, int op, int family, int adj_ctas_per_sm);
-int fock_plan_op_config(const fock_plan* plan, int op, int* family, int* adj_ctas_per_sm, int* plane_ok);
+int fock_plan_tune(fock_plan* plan, int op, int family, int adj_ctas_per_sm, int plane_tile_columns);
+int fock_plan_op_config(const fock_plan* plan, int op, int* family, int* adj_ctas_per_sm, int* plane_ok,
+                        int* plane_tile_columns);
 
 /* Persistent sweeps.  A single-circuit complex64 plan whose state is at most
  * FOCK_GB300_SWEEP_MAX_BYTES bytes (read at plan creation; default 0 = off,

@@ -90,9 +90,9 @@ _SIGS = {
     "fock_plan_op_times": (_i, [_vp, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "fock_plan_sweep_status": (_i, [_vp, _vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "fock_wigner": (_i, [_i, _vp, _vp, _i, _vp, _i, ctypes.c_double, _vp, _vp]),
-    "fock_plan_tune": (_i, [_vp, _i, _i, _i]),
+    "fock_plan_tune": (_i, [_vp, _i, _i, _i, _i]),
     "fock_plan_op_config": (_i, [_vp, _i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
-                                 ctypes.POINTER(ctypes.c_int)]),
+                                 ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
 }
 
 _lock = threading.Lock()

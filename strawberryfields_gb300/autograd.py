@@ -208,19 +208,21 @@ class CompiledCircuit:
         return grads, lam
 
     def op_config(self, k):
-        """(family, adjoint CTAs per SM, plane_ok) of fused op k: family 0 is
-        the block kernels, 1 the plane-tile kernels."""
-        fam, ctas, ok = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        """(family, adjoint CTAs per SM, plane_ok, plane tile columns) of
+        fused op k: family 0 is the block kernels, 1 the plane-tile kernels."""
+        fam, ctas, ok, tc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         L.check(L.load().fock_plan_op_config(self._plan, int(k), ctypes.byref(fam), ctypes.byref(ctas),
-                                             ctypes.byref(ok)), "fock_plan_op_config")
-        return fam.value, ctas.value, bool(ok.value)
+                                             ctypes.byref(ok), ctypes.byref(tc)), "fock_plan_op_config")
+        return fam.value, ctas.value, bool(ok.value), tc.value
 
-    def tune_op(self, k, family=-1, ctas_per_sm=0):
-        """Select op k's kernel family (-1 keeps it) and block-adjoint CTAs
-        per SM (0 keeps it).  Reallocates the workspace on the next sweep;
-        graphs captured before the change are stale."""
+    def tune_op(self, k, family=-1, ctas_per_sm=0, tile_columns=0):
+        """Select op k's kernel family (-1 keeps it), block-adjoint CTAs per
+        SM and plane tile columns of a two-mode op (0 keeps them).
+        Reallocates the workspace on the next sweep; graphs captured before
+        the change are stale."""
         torch.cuda.synchronize(self.device)
-        L.check(L.load().fock_plan_tune(self._plan, int(k), int(family), int(ctas_per_sm)), "fock_plan_tune")
+        L.check(L.load().fock_plan_tune(self._plan, int(k), int(family), int(ctas_per_sm), int(tile_columns)),
+                "fock_plan_tune")
         info = L.PlanInfo()
         L.check(L.load().fock_plan_get_info(self._plan, ctypes.byref(info)), "fock_plan_get_info")
         self.info = info
@@ -250,14 +252,15 @@ class CompiledCircuit:
                 best_b = [min(a, b) for a, b in zip(best_b, bbuf)]
         return (best_f, best_b) if per_op else best
 
-    def autotune(self, params, ctas=(2, 4, 8, 16), repeats=3):
-        """Pick each op's kernel family and block-adjoint CTAs per SM by
-        timing a forward + adjoint sweep at ``params`` under every candidate
-        (per-op CUDA events, best of ``repeats``), keeping per op the
-        candidate with the smallest forward + adjoint time.  The tuned plan
-        is kept only when its whole step (PDL launches, final reduction) is
-        faster than the configuration it started from.  Returns
-        ``(configs, ms_before, ms_after)`` with configs[k] = (family, ctas)."""
+    def autotune(self, params, ctas=(2, 4, 8, 16), tiles=(32, 24), repeats=3):
+        """Pick each op's kernel family, block-adjoint CTAs per SM and plane
+        tile columns by timing a forward + adjoint sweep at ``params`` under
+        every candidate (per-op CUDA events, best of ``repeats``), keeping per
+        op the candidate with the smallest forward + adjoint time.  The tuned
+        plan is kept only when its whole step (PDL launches, final reduction)
+        is faster than the configuration it started from.  Returns
+        ``(configs, ms_before, ms_after)`` with configs[k] =
+        (family, ctas, tile columns)."""
         if self.n_ops == 0:
             return [], 0.0, 0.0
         lib = L.load()
@@ -269,33 +272,48 @@ class CompiledCircuit:
         n = self.n_ops
         start = [self.op_config(k) for k in range(n)]
         ms_before = self._timed_sweeps(p, lam, repeats, False)
-        cands = [(0, int(c)) for c in ctas]
-        if any(ok for _, _, ok in start):
-            cands.append((1, 0))
+        cands = [(0, int(c), 0) for c in ctas]
+        if any(ok for _, _, ok, _ in start):
+            cands += [(1, 0, int(t)) for t in tiles]
         cost = [dict() for _ in range(n)]
         L.check(lib.fock_plan_enable_timing(self._plan, 1), "fock_plan_enable_timing")
         try:
-            for fam, c in cands:
+            for fam, c, tc in cands:
                 for k in range(n):
                     if fam == 0 or start[k][2]:
-                        self.tune_op(k, fam, c)
+                        self.tune_op(k, fam, c, tc if start[k][3] <= 32 else 0)
                     else:
                         self.tune_op(k, 0, start[k][1])
                 f, b = self._timed_sweeps(p, lam, repeats, True)
                 for k in range(n):
                     if fam == 0 or start[k][2]:
-                        cost[k][(fam, c)] = f[k] + b[k]
+                        cost[k][(fam, c, tc)] = f[k] + b[k]
         finally:
             L.check(lib.fock_plan_enable_timing(self._plan, 0), "fock_plan_enable_timing")
         best = [min(ck, key=ck.get) for ck in cost]
-        for k, (fam, c) in enumerate(best):
-            self.tune_op(k, fam, c if fam == 0 else start[k][1])
-        ms_after = self._timed_sweeps(p, lam, repeats, False)
-        if ms_after > ms_before:
-            for k, (fam, c, _) in enumerate(start):
-                self.tune_op(k, fam, c)
-        self.tuned = [(fam, c) for fam, c, _ in (self.op_config(k) for k in range(n))]
-        return self.tuned, ms_before, min(ms_before, ms_after)
+
+        def tile(k, tc):
+            return tc if start[k][3] <= 32 else 0
+
+        def apply(cfg):
+            for k, (fam, c, tc) in enumerate(cfg):
+                self.tune_op(k, fam, c, tile(k, tc))
+
+        # whole-step check of the per-op picks, of the picks with the
+        # starting CTA densities (per-op events run without programmatic
+        # dependent launch, which favours other densities), and of the start
+        start_cfg = [(fam, c, tc) for fam, c, _, tc in start]
+        picks = [(fam, c if fam == 0 else start[k][1], tc) for k, (fam, c, tc) in enumerate(best)]
+        no_ctas = [(fam, start[k][1], tc) for k, (fam, c, tc) in enumerate(picks)]
+        results = [(ms_before, start_cfg)]
+        for cfg in (picks, no_ctas):
+            if cfg != start_cfg and all(cfg != r[1] for r in results):
+                apply(cfg)
+                results.append((self._timed_sweeps(p, lam, repeats, False), cfg))
+        ms_after, cfg = min(results, key=lambda r: r[0])
+        apply(cfg)
+        self.tuned = [(fam, c, tc) for fam, c, _, tc in (self.op_config(k) for k in range(n))]
+        return self.tuned, ms_before, ms_after
 
     def sweep_status(self):
         """(persistent, error): whether this plan runs its sweeps as single

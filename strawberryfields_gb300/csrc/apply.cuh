@@ -335,7 +335,9 @@ struct PlaneGeom {
   unsigned short items[PL_MAX_ITEMS];  // (block << 4) | column group, per warp
 };
 // 0 when the op does not fit the plane kernels (then the block kernels run)
-int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, int adjoint, PlaneGeom* g);
+// tile_columns: columns per tile of a two-mode plane op (0: 32)
+int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, int adjoint, PlaneGeom* g,
+                    int tile_columns = 0);
 int plane_grid(int dtype, const PlaneGeom& g, int adjoint, int nb);
 // the ops the plane kernels run by default (the others keep the block kernels)
 int plane_preferred(int layout, const AxisView& v);

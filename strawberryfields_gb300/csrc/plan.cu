@@ -48,6 +48,7 @@ struct PlanOp {
   PlaneGeom pg_fwd, pg_adj;
   int grid_fwd = 0, grid_adj = 0;
   int adj_ctas = 8;  // adjoint CTAs per SM (block kernels)
+  int pl_tc = 0;     // plane-tile columns of a two-mode op (0: the default 32)
   // persistent-sweep adjoint schedule and partial-sum region
   AdjSched psched;
   int64_t ppart_off = 0;
@@ -903,13 +904,27 @@ extern "C" int fock_plan_backward_recompute(fock_plan* P, const double* params, 
   return param_grads(P, ws, c, grad_params, st);
 }
 
-extern "C" int fock_plan_tune(fock_plan* P, int k, int family, int adj_ctas_per_sm) {
+extern "C" int fock_plan_tune(fock_plan* P, int k, int family, int adj_ctas_per_sm, int plane_tile_columns) {
   if (!P || k < 0 || k >= (int)P->ops.size()) return fock_set_error(FOCK_ERR_INVALID, "bad op index");
   PlanOp& op = P->ops[k];
   if (family > 1) return fock_set_error(FOCK_ERR_INVALID, "kernel family must be 0 (block) or 1 (plane)");
   if (family == 1 && !op.plane_ok) return fock_set_error(FOCK_ERR_UNSUPPORTED, "op %d has no plane-tile kernel", k);
   if (adj_ctas_per_sm < 0 || adj_ctas_per_sm > 64)
     return fock_set_error(FOCK_ERR_INVALID, "adjoint CTAs per SM must be in [1, 64]");
+  if (plane_tile_columns && (plane_tile_columns < 8 || plane_tile_columns > 32))
+    return fock_set_error(FOCK_ERR_INVALID, "plane tile columns must be in [8, 32]");
+  if (plane_tile_columns && op.plane_ok && op.layout != LAYOUT_DENSE && plane_tile_columns != (op.pl_tc ? op.pl_tc : 32)) {
+    PlaneGeom f, a;
+    if (!make_plane_geom(P->dtype, op.view, P->D, op.layout, op.swap, 0, &f, plane_tile_columns) ||
+        !make_plane_geom(P->dtype, op.view, P->D, op.layout, op.swap, 1, &a, plane_tile_columns))
+      return fock_set_error(FOCK_ERR_UNSUPPORTED, "op %d: no plane geometry with %d tile columns", k,
+                            plane_tile_columns);
+    op.pg_fwd = f;
+    op.pg_adj = a;
+    op.grid_fwd = plane_grid(P->dtype, f, 0, P->batch);
+    op.grid_adj = plane_grid(P->dtype, a, 1, P->batch);
+    op.pl_tc = plane_tile_columns;
+  }
   if (family >= 0) op.plane = family;
   if (adj_ctas_per_sm > 0) {
     op.adj_ctas = adj_ctas_per_sm;
@@ -919,12 +934,14 @@ extern "C" int fock_plan_tune(fock_plan* P, int k, int family, int adj_ctas_per_
   return FOCK_OK;
 }
 
-extern "C" int fock_plan_op_config(const fock_plan* P, int k, int* family, int* adj_ctas_per_sm, int* plane_ok) {
+extern "C" int fock_plan_op_config(const fock_plan* P, int k, int* family, int* adj_ctas_per_sm, int* plane_ok,
+                                   int* plane_tile_columns) {
   if (!P || k < 0 || k >= (int)P->ops.size()) return fock_set_error(FOCK_ERR_INVALID, "bad op index");
   const PlanOp& op = P->ops[k];
   if (family) *family = op.plane;
   if (adj_ctas_per_sm) *adj_ctas_per_sm = op.adj_ctas;
   if (plane_ok) *plane_ok = op.plane_ok;
+  if (plane_tile_columns) *plane_tile_columns = op.plane_ok ? op.pg_fwd.TC : 0;
   return FOCK_OK;
 }
 

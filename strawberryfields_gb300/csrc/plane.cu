@@ -400,7 +400,8 @@ __global__ void __launch_bounds__(PL_THREADS, 2)
 // ---------------------------------------------------------------------------
 static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, int adjoint, PlaneGeom* out) {
+int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, int adjoint, PlaneGeom* out,
+                    int tile_columns) {
   PlaneGeom g;
   memset(&g, 0, sizeof(g));
   const int esz = dtype == FOCK_C64 ? 8 : 16;
@@ -454,13 +455,17 @@ int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, i
   if (g.nslot > PL_THREADS * pl_kmax(D)) return 0;
   // columns per tile: one warp of columns per block for two modes; enough
   // column groups to give every warp a dense block otherwise
-  g.TC = g.two ? 32 : 256;
+  // two-mode planes: tile_columns (8..32; default 32) -- fewer columns give
+  // smaller tiles and more resident CTAs, which pays on L2-resident states
+  // (the autotuner picks it per op)
+  if (tile_columns && (tile_columns < 8 || tile_columns > 32)) return 0;
+  g.TC = g.two ? (tile_columns ? tile_columns : 32) : 256;
   const size_t tile_cap = adjoint ? 96 * 1024 : 72 * 1024;  // both buffers
   while (g.TC > 32 && (size_t)2 * g.TC * g.EP * esz > tile_cap) g.TC >>= 1;
   g.ntiles = (g.ncols + g.TC - 1) / g.TC;
   if (g.flat && (int64_t)g.TC * g.E >= (1 << 16)) return 0;
   // warp items (block, column group), longest first onto the least loaded warp
-  const int ncg = g.TC / 32;
+  const int ncg = (g.TC + 31) / 32;
   std::vector<std::pair<int, int>> items;  // (cost, item)
   for (int y = 0; y < g.nblk; ++y)
     for (int c = 0; c < ncg; ++c) items.push_back({g.s[y] * g.s[y], (y << 4) | c});

@@ -175,30 +175,36 @@ def test_plan_tune_knobs(lib):
     info, ops = _ops(plan)
 
     def cfg(k):
-        f, c, ok = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-        assert lib.fock_plan_op_config(plan, k, ctypes.byref(f), ctypes.byref(c), ctypes.byref(ok)) == 0
-        return f.value, c.value, ok.value
+        f, c, ok, tc = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        assert lib.fock_plan_op_config(plan, k, ctypes.byref(f), ctypes.byref(c), ctypes.byref(ok),
+                                       ctypes.byref(tc)) == 0
+        return f.value, c.value, ok.value, tc.value
 
     configs = [cfg(k) for k in range(info.n_ops)]
-    assert all(c == 8 for _, c, _ in configs)
-    assert any(ok for _, _, ok in configs)
-    assert lib.fock_plan_tune(plan, 0, 2, 0) == _lib.FOCK_ERR_INVALID
-    assert lib.fock_plan_tune(plan, 0, -1, 65) == _lib.FOCK_ERR_INVALID
-    assert lib.fock_plan_tune(plan, info.n_ops, -1, 4) == _lib.FOCK_ERR_INVALID
+    assert all(c == 8 for _, c, _, _ in configs)
+    assert any(ok for _, _, ok, _ in configs)
+    two = [k for k, o in enumerate(ops) if o[0] == 2 and configs[k][2]]
+    assert two and all(configs[k][3] == 32 for k in two)
+    assert lib.fock_plan_tune(plan, 0, 2, 0, 0) == _lib.FOCK_ERR_INVALID
+    assert lib.fock_plan_tune(plan, 0, -1, 65, 0) == _lib.FOCK_ERR_INVALID
+    assert lib.fock_plan_tune(plan, 0, -1, 0, 40) == _lib.FOCK_ERR_INVALID
+    assert lib.fock_plan_tune(plan, info.n_ops, -1, 4, 0) == _lib.FOCK_ERR_INVALID
     ws0 = info.workspace_bytes
     sizes = []
     for ctas in (2, 16):
         for k in range(info.n_ops):
-            assert lib.fock_plan_tune(plan, k, 0, ctas) == 0
+            assert lib.fock_plan_tune(plan, k, 0, ctas, 0) == 0
         sizes.append(_ops(plan)[0].workspace_bytes)
     assert sizes[1] > sizes[0] and cfg(0)[:2] == (0, 16)
+    # plane tiles of 24 columns on a two-mode op (its plane partial sums follow its grid)
+    assert lib.fock_plan_tune(plan, two[0], 1, 0, 24) == 0 and cfg(two[0])[3] == 24
     for k in range(info.n_ops):
-        assert lib.fock_plan_tune(plan, k, configs[k][0], configs[k][1]) == 0
-    assert _ops(plan)[0].workspace_bytes == ws0
+        assert lib.fock_plan_tune(plan, k, configs[k][0], configs[k][1], configs[k][3] if configs[k][3] <= 32 else 0) == 0
+    assert _ops(plan)[0].workspace_bytes == ws0 and cfg(two[0])[3] == 32
     lib.fock_plan_destroy(plan)
     # two-mode plane tiles stop at cutoff 16: a cutoff-18 beamsplitter has none
     rc, plan = _plan([(5, 0, 1, 0)], 2, N=2, D=18)
-    assert rc == 0 and lib.fock_plan_tune(plan, 0, 1, 0) == _lib.FOCK_ERR_UNSUPPORTED
+    assert rc == 0 and lib.fock_plan_tune(plan, 0, 1, 0, 0) == _lib.FOCK_ERR_UNSUPPORTED
     lib.fock_plan_destroy(plan)
 
 

@@ -293,15 +293,16 @@ def test_tuned_kernels_give_the_same_gradient(cuda):
     ref_s = c.forward_states(p)
     ref_g = c.backward(p, ref_s, g_state)[0]
     start = [c.op_config(k) for k in range(c.n_ops)]
-    assert any(ok for _, _, ok in start)
-    for fam, ctas in [(0, 1), (0, 3), (0, 16), (1, 0)]:
+    assert any(ok for _, _, ok, _ in start)
+    for fam, ctas, tc in [(0, 1, 0), (0, 3, 0), (0, 16, 0), (1, 0, 0), (1, 0, 24), (1, 0, 8)]:
         for k in range(c.n_ops):
-            c.tune_op(k, fam if (fam == 0 or start[k][2]) else 0, ctas)
+            two = start[k][2] and start[k][3] <= 32
+            c.tune_op(k, fam if (fam == 0 or start[k][2]) else 0, ctas, tc if two else 0)
         s = c.forward_states(p)
-        assert torch.allclose(s, ref_s, rtol=0, atol=1e-13), (fam, ctas)
+        assert torch.allclose(s, ref_s, rtol=0, atol=1e-13), (fam, ctas, tc)
         g = c.backward(p, s, g_state)[0]
-        assert torch.allclose(g, ref_g, rtol=1e-11, atol=1e-13), (fam, ctas)
-    configs, before, after = c.autotune(p, ctas=(2, 8), repeats=1)
+        assert torch.allclose(g, ref_g, rtol=1e-11, atol=1e-13), (fam, ctas, tc)
+    configs, before, after = c.autotune(p, ctas=(2, 8), tiles=(32, 16), repeats=1)
     assert len(configs) == c.n_ops and after <= before
     s = c.forward_states(p)
     g = c.backward(p, s, g_state)[0]
