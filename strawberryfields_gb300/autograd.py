@@ -252,7 +252,7 @@ class CompiledCircuit:
                 best_b = [min(a, b) for a, b in zip(best_b, bbuf)]
         return (best_f, best_b) if per_op else best
 
-    def autotune(self, params, ctas=(2, 4, 8, 16), tiles=(32, 24), repeats=3):
+    def autotune(self, params, ctas=(2, 4, 6, 8, 12, 16), tiles=(32, 24, 16), repeats=3):
         """Pick each op's kernel family, block-adjoint CTAs per SM and plane
         tile columns by timing a forward + adjoint sweep at ``params`` under
         every candidate (per-op CUDA events, best of ``repeats``), keeping per
