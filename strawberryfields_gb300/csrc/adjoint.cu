@@ -34,9 +34,14 @@ __global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)
                          double2* __restrict__ cpart, AdjSched sc, int write_lam, BatchArg bt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // which block this CTA serves, and its rank x among that block's CTAs
-  int y = 0;
-  while (y + 1 < sc.nblk && (int)blockIdx.x >= sc.start[y + 1]) ++y;
-  const int xrank = (int)blockIdx.x - sc.start[y];
+  int y = 0, xrank;
+  if (sc.interleave) {
+    y = (int)blockIdx.x % sc.nblk;
+    xrank = (int)blockIdx.x / sc.nblk;
+  } else {
+    while (y + 1 < sc.nblk && (int)blockIdx.x >= sc.start[y + 1]) ++y;
+    xrank = (int)blockIdx.x - sc.start[y];
+  }
   const int gxb = sc.gx[y];
   psi_in += blockIdx.z * bt.state_stride;
   lam_out += blockIdx.z * bt.state_stride;
@@ -91,6 +96,9 @@ AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout, int nb,
   }
   sc.start[sc.nblk] = start;
   sc.total = start;
+  // every block has the same CTA count, so the interleaved order is a
+  // permutation of the same grid
+  sc.interleave = interleave_blocks(layout, v);
   // partial offsets by stored block index (gx depends only on the block size,
   // so a block and its mirror image have the same count)
   for (int bs = 0; bs < sc.nblk; ++bs) {

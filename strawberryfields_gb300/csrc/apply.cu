@@ -53,15 +53,18 @@ AxisView make_view2(int naxes, int D, int ax1, int ax2) {
 template <typename CT, int DMAX>
 __global__ void __launch_bounds__(APPLY_THREADS, ApplyMinBlocks<DMAX>::value) apply_block_kernel(
     const CT* __restrict__ in, CT* __restrict__ out, AxisView v, int D, int layout, const double2* __restrict__ mat,
-    int mflags, BatchArg bt) {
+    int mflags, BatchArg bt, int il) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   CT* Ms = reinterpret_cast<CT*>(smem_raw);
   in += blockIdx.z * bt.state_stride;
   out += blockIdx.z * bt.state_stride;
   mat += blockIdx.z * bt.mat_stride;
-  const int b = layout == LAYOUT_DENSE ? 0 : block_of_y(D, blockIdx.y);
+  // grid (column tiles, blocks) or, interleaved (il), (blocks, column tiles)
+  const int yb = il ? (int)blockIdx.x : (int)blockIdx.y;
+  const int64_t tile = il ? (int64_t)blockIdx.y : (int64_t)blockIdx.x;
+  const int b = layout == LAYOUT_DENSE ? 0 : block_of_y(D, yb);
   const BlockGeom g = block_geom(v, D, layout, b, (mflags & MF_SWAP) ? 1 : 0);
-  const int64_t j0 = (int64_t)blockIdx.x * (APPLY_THREADS * APPLY_COLS) + threadIdx.x;
+  const int64_t j0 = tile * (APPLY_THREADS * APPLY_COLS) + threadIdx.x;
   pdl_wait();
   pdl_launch_dependents();
   ApplyDispatch<CT, kSStep, DMAX>::run(in, out, v, D, Ms, mat, mflags, g, j0);
@@ -74,12 +77,14 @@ static int launch_apply_t(const void* in, void* out, const AxisView& v, int D, i
   const int64_t gx = (v.ncols + APPLY_THREADS * APPLY_COLS - 1) / (APPLY_THREADS * APPLY_COLS);
   if (gx > 0x7fffffffLL) return fock_set_error(FOCK_ERR_INVALID, "state too large");
   if (bt.nb < 1 || bt.nb > 65535) return fock_set_error(FOCK_ERR_INVALID, "batch of %d circuits", bt.nb);
-  dim3 grid((unsigned)gx, nblk, bt.nb);
+  // blocks of one column tile next to each other when they share sectors
+  const bool il = interleave_blocks(layout, v) && gx > 1 && gx <= 65535;
+  dim3 grid(il ? (unsigned)nblk : (unsigned)gx, il ? (unsigned)gx : (unsigned)nblk, bt.nb);
   const size_t sm = ms_slots(sizeof(CT) == 8 ? FOCK_C64 : FOCK_C128, D) * sizeof(CT);
   auto k = apply_block_kernel<CT, DMAX>;
   if (sm > 48 * 1024) FOCK_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   FOCK_CUDA_TRY(launch_kernel(k, grid, dim3(APPLY_THREADS), sm, st, bt.pdl, (const CT*)in, (CT*)out, v, D, layout,
-                               mat, mflags, bt));
+                               mat, mflags, bt, (int)il));
   return FOCK_OK;
 }
 

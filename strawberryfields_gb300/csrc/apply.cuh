@@ -278,6 +278,11 @@ int launch_apply(int dtype, const void* in, void* out, const AxisView& v, int D,
 struct AdjSched {
   int nblk;
   int total;
+  // CTA order: 0 -> block by block (CTA x serves block y for
+  // start[y] <= x < start[y+1]); 1 -> interleaved, CTA x serves block
+  // x % nblk with rank x / nblk (every block has gx[0] CTAs), so the CTAs of
+  // all blocks that read the same columns run together
+  int interleave;
   int64_t part_entries;
   int gx[ADJ_MAX_BLOCKS];
   int start[ADJ_MAX_BLOCKS + 1];
@@ -287,6 +292,13 @@ struct AdjSched {
 // SM the launch spreads over all blocks and circuits (the default measured
 // best for the 6-mode cutoff-12 QNN; fock_plan_tune changes it per op)
 AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout, int nb = 1, int ctas_per_sm = 8);
+// two-mode ops on the innermost axis pair (C = 1) run their block CTAs
+// interleaved: each block reads a few elements of every sector of the
+// columns' planes, so the blocks that share a plane should read it together
+// (from L2) rather than one block after another (from DRAM)
+__host__ __device__ __forceinline__ int interleave_blocks(int layout, const AxisView& v) {
+  return layout != LAYOUT_DENSE && v.C == 1;
+}
 int launch_adjoint_partials(int dtype, const void* psi_in, const void* lam_out, void* lam_in,
                             const AxisView& v, int D, int layout, const double2* mat, int mflags,
                             double2* cpart, const AdjSched& sc, cudaStream_t st, const BatchArg& bt = BatchArg());
