@@ -84,10 +84,20 @@ AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout, int nb,
   // circuits of a batch (grid.z); largest blocks come first in the flat grid
   // so they start first
   const int target = std::max(1, std::max(ctas_per_sm, 1) * fock_num_sms() / std::max(nb, 1));
+  // innermost-pair ops: one column tile per CTA, so the CTAs of all blocks
+  // that read a tile's planes run together (a CTA that walks many tiles
+  // drifts away from the other blocks' CTAs, and the planes come from DRAM
+  // again) -- as far as 64 MB of partial sums per launch allow
+  int64_t per_block = (target + sc.nblk - 1) / sc.nblk;
+  if (interleave_blocks(layout, v)) {
+    const int64_t per_tile = (layout == LAYOUT_DENSE ? (int64_t)D * D : blk_total(D)) * (int64_t)sizeof(double2) *
+                             std::max(nb, 1);
+    per_block = std::max<int64_t>(per_block, std::min<int64_t>(ntiles, (64ll << 20) / per_tile));
+  }
   int64_t part = 0;
   int start = 0;
   for (int y = 0; y < sc.nblk; ++y) {
-    int64_t g = (target + sc.nblk - 1) / sc.nblk;
+    int64_t g = per_block;
     if (g < 1) g = 1;
     if (g > ntiles) g = ntiles;
     sc.gx[y] = (int)g;
