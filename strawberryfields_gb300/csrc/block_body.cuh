@@ -35,9 +35,11 @@ __device__ __forceinline__ void apply_cols(const CT* __restrict__ in, CT* __rest
   const int64_t b0 = valid ? col_base(v, j0, D) + g.boff : 0;
   CT x0[S];
   // complex64 column contiguous in memory (a one-mode op on the innermost
-  // axis) with an even length on a 16-byte boundary: 16-byte loads and
+  // axis) with an even length on a 16-byte boundary (checked on the
+  // addresses: a state may start at any 8-byte offset): 16-byte loads and
   // stores of element pairs, half the memory instructions
-  const bool pairs = sizeof(CT) == 8 && g.step == 1 && !(s & 1) && !(b0 & 1);
+  const bool pairs = sizeof(CT) == 8 && g.step == 1 && !(s & 1) &&
+                     !(((uintptr_t)(in + b0) | (uintptr_t)(out + b0)) & 15);
   if (valid) {
     if constexpr (sizeof(CT) == 8) {
       if (pairs) {

@@ -346,3 +346,27 @@ def test_plane_kernels_on_every_op_match_oracle(cuda, D, dtype):
     assert np.abs(psi.detach().to(torch.complex128).cpu().numpy() - ref_states[-1]).max() < tol_s
     got = p.grad.cpu().numpy()
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < tol_g
+
+
+def test_state_at_an_8_byte_offset(cuda):
+    """A complex64 input state that starts 8 bytes past a 16-byte boundary
+    (a slice of a larger buffer): the one-mode op on the innermost axis
+    takes its 8-byte path there and gives the oracle's result."""
+    import torch
+    from strawberryfields_gb300 import CompiledCircuit
+
+    N, D = 3, 6
+    gates = [(4, 2, -1, 0), (5, 1, 2, 2)]  # squeezer on the last mode, then a beamsplitter
+    params = np.array([0.3, 0.7, 0.5, 0.2])
+    rng = np.random.default_rng(4)
+    psi = rng.normal(size=(D,) * N) + 1j * rng.normal(size=(D,) * N)
+    psi /= np.linalg.norm(psi)
+    big = torch.zeros(D ** N + 1, dtype=torch.complex64, device="cuda")
+    big[1:] = torch.as_tensor(psi.reshape(-1), device="cuda").to(torch.complex64)
+    x = big[1:].reshape([D] * N)
+    assert x.data_ptr() % 16 == 8
+    circ = CompiledCircuit(N, D, gates, 4, dtype=torch.complex64)
+    p = torch.tensor(params, device="cuda", dtype=torch.float64)
+    out = circ.forward_states(p, state_in=x, store_all=False)
+    ref = fo.run_gates(gates, params, N, D, psi)[-1]
+    assert np.abs(out.to(torch.complex128).cpu().numpy() - ref).max() < 1e-5
