@@ -661,7 +661,7 @@ def batched_case(args):
     n = args.circuits
     t0 = time.perf_counter()
     circuits, params = random_qnn_batch(n, seed=0)
-    cb = CircuitBatch(circuits, dtype=torch.complex64, device=dev, streams=8)
+    cb = CircuitBatch(circuits, dtype=torch.complex64, device=dev, streams=args.streams)
     setup_s = time.perf_counter() - t0
     targets = {}
     for nm, D, _, _ in circuits:
@@ -720,6 +720,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--case", default="gradient", choices=["gradient", "single-gate", "batched", "lossy"])
     ap.add_argument("--circuits", type=int, default=4096)
+    ap.add_argument("--streams", type=int, default=8, help="batched case: CUDA streams the groups are spread over")
     ap.add_argument("--only", default="", help="single-gate case: comma-separated subset of the kernels")
     ap.add_argument("--modes", type=int, default=7, help="single-gate case: modes of the ket")
     ap.add_argument("--cutoff", type=int, default=12, help="single-gate case: cutoff of the ket")
