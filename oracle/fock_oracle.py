@@ -25,7 +25,11 @@ What it restates (complex128 / FP64 throughout, like the reference):
   the reference's per-fibre Python loops (same arithmetic, same index order);
 * readouts of ``strawberryfields/backends/states.py`` (``all_fock_probs`` :580,
   ``fock_prob`` :644, ``reduced_dm`` :613, ``mean_photon`` :657) computed from
-  marginals instead of the full density matrix, and ``wigner`` :730.
+  marginals instead of the full density matrix, and ``wigner`` :730;
+* the TF backend's Gaussian gate (``tfbackend/ops.py:457-572``): ``choi_trick``
+  and the renormalised multidimensional Hermite tensor of the third-party
+  thewalrus (not vendored; restated from its recurrence), pinned against the
+  exact single- and two-mode gate matrices.
 
 Parity of these restatements is pinned by ``tests/test_oracle.py`` against
 ``scipy.linalg.expm`` of each gate generator, against the reference's own
