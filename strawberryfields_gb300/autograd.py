@@ -303,7 +303,9 @@ class CompiledCircuit:
         # starting CTA densities (per-op events run without programmatic
         # dependent launch, which favours other densities), and of the start
         start_cfg = [(fam, c, tc) for fam, c, _, tc in start]
-        picks = [(fam, c if fam == 0 else start[k][1], tc) for k, (fam, c, tc) in enumerate(best)]
+        # (an op left on block kernels keeps its starting plane tile)
+        picks = [(fam, c if fam == 0 else start[k][1], tc if fam == 1 else start[k][3])
+                 for k, (fam, c, tc) in enumerate(best)]
         no_ctas = [(fam, start[k][1], tc) for k, (fam, c, tc) in enumerate(picks)]
         results = [(ms_before, start_cfg)]
         for cfg in (picks, no_ctas):

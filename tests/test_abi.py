@@ -215,3 +215,68 @@ def test_product_path_has_no_cpu_fallback():
         if fn.endswith(".py"):
             src = open(os.path.join(pkg, fn)).read()
             assert "oracle" not in re.sub(r"#.*|\"\"\"[\s\S]*?\"\"\"", "", src), fn
+
+
+def test_autotune_selection_logic(monkeypatch):
+    """CompiledCircuit.autotune's choice, with the device replaced by a cost
+    model (no GPU): per op the cheapest candidate, then the whole-step check
+    that falls back to the starting CTA densities when the per-op picks lose
+    on the whole step."""
+    import types
+
+    from strawberryfields_gb300 import autograd
+
+    class FakeLib:
+        def fock_plan_enable_timing(self, plan, on):
+            return 0
+
+    monkeypatch.setattr(autograd.L, "load", lambda: FakeLib())
+
+    # op 0: dense, no plane kernel; op 1: two-mode, plane by default; op 2: two-mode on block kernels
+    start = [(0, 8, False, 256), (1, 8, True, 32), (0, 8, True, 32)]
+    best_ctas = {0: 4, 2: 16}
+
+    def op_cost(k, cfg):
+        fam, c, tc = cfg
+        if k == 1:
+            return 5.0 if (fam == 1 and tc == 24) else 6.0 if fam == 1 else 9.0
+        if fam == 1:
+            return 8.0
+        return 2.0 if c == best_ctas[k] else 3.0
+
+    class Fake(autograd.CompiledCircuit):
+        def __init__(self, penalty):
+            self.info = types.SimpleNamespace(n_ops=3)
+            self._bshape = [2, 2]
+            self.dtype = torch.complex64
+            self.device = torch.device("cpu")
+            self._plan = None
+            self.cfg = [(f, c, tc) for f, c, _, tc in start]
+            self.penalty = penalty
+
+        def _params(self, params):
+            return params
+
+        def op_config(self, k):
+            f, c, tc = self.cfg[k]
+            return f, c, start[k][2], tc if tc else start[k][3]
+
+        def tune_op(self, k, family=-1, ctas_per_sm=0, tile_columns=0):
+            f, c, tc = self.cfg[k]
+            self.cfg[k] = (family if family >= 0 else f, ctas_per_sm or c, tile_columns or tc)
+
+        def _timed_sweeps(self, p, lam, repeats, per_op):
+            costs = [op_cost(k, self.cfg[k]) for k in range(3)]
+            if per_op:
+                return costs, [0.0] * 3
+            # the whole step: PDL penalises CTA densities other than 8 by `penalty` each
+            return sum(costs) + self.penalty * sum(1 for f, c, _ in self.cfg if f == 0 and c != 8)
+
+    import torch
+
+    c = Fake(penalty=0.0)
+    cfgs, before, after = c.autotune(None, ctas=(4, 8, 16), tiles=(32, 24))
+    assert cfgs == [(0, 4, 256), (1, 8, 24), (0, 16, 32)] and after < before
+    c = Fake(penalty=5.0)  # the CTA picks lose on the whole step: keep densities, take the tile
+    cfgs, before, after = c.autotune(None, ctas=(4, 8, 16), tiles=(32, 24))
+    assert cfgs == [(0, 8, 256), (1, 8, 24), (0, 8, 32)] and after < before
