@@ -358,3 +358,22 @@ def test_gaussian_host_choi_matches_oracle():
         gaussian.check_gate(S * 1.1, d)
     with pytest.raises(ValueError, match="compatible"):
         gaussian.check_gate(S, d[:2])
+
+
+def test_gaussian_choi_parameters_of_the_identity_and_a_displacement():
+    """S = I, d = 0 is the identity gate: R couples each output index to its
+    input index only (R = [[0, -I], [-I, 0]], so the Hermite tensor is
+    delta(out, in)), y = 0, C = 1.  A pure displacement keeps that R and
+    gives y = (alpha, -conj(alpha)), C = exp(-|alpha|^2 / 2) = <0|D(alpha)|0>."""
+    from strawberryfields_gb300 import gaussian
+
+    for m in (1, 2, 3):
+        R, y, C = gaussian.choi_parameters(np.eye(2 * m), np.zeros(2 * m))
+        R_id = -np.block([[np.zeros((m, m)), np.eye(m)], [np.eye(m), np.zeros((m, m))]])
+        assert np.abs(R - R_id).max() < 1e-14 and np.abs(y).max() < 1e-14 and abs(C - 1) < 1e-14
+    d = np.array([0.4, -0.2, 0.6, 0.1])  # (x1, x2, p1, p2): alpha = (x + i p) / 2
+    R, y, C = gaussian.choi_parameters(np.eye(4), d)
+    alpha = (d[:2] + 1j * d[2:]) / 2
+    assert np.abs(R + np.block([[np.zeros((2, 2)), np.eye(2)], [np.eye(2), np.zeros((2, 2))]])).max() < 1e-14
+    assert np.abs(y[:2] - alpha).max() < 1e-14 and np.abs(y[2:] + alpha.conj()).max() < 1e-14
+    assert abs(C - np.exp(-0.5 * np.sum(np.abs(alpha) ** 2))) < 1e-14
