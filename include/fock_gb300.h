@@ -161,12 +161,16 @@ int64_t fock_reduced_dm1_workspace_bytes(int num_modes, int cutoff, int pure, in
  * memory (no workspace argument).  No counterpart in the reference.  The
  * reduction's partial sums live in a fixed 512 KiB array in device global
  * memory owned by the library (held by every GPU that loads it until exit),
- * which bounds the cutoff to <= 60; larger cutoffs are rejected with
- * FOCK_ERR_INVALID.  The first call on a device looks up that array's device
- * address (cudaGetSymbolAddress) with the device current: make that first
- * call before any stream capture.  All calls share the array, so calls that
- * overlap on the GPU (different streams, or concurrent host threads) race;
- * serialise them.  Allocates nothing: no cudaMalloc/cudaFree. */
+ * which bounds the cutoff to <= FOCK_NOALLOC_MAX_CUTOFF; larger cutoffs are
+ * rejected with FOCK_ERR_INVALID.  Each call outside stream capture looks up
+ * that array's device address (cudaGetSymbolAddress) with the device current;
+ * a call made while `stream` is capturing uses the address found by the last
+ * uncaptured call on the device, so make one call before any stream capture
+ * (and again after a cudaDeviceReset before capturing).  All calls share the
+ * array, so calls that overlap on the GPU (different streams, or concurrent
+ * host threads) race; serialise them.  Allocates nothing: no
+ * cudaMalloc/cudaFree. */
+#define FOCK_NOALLOC_MAX_CUTOFF 60
 int fock_reduced_dm1_noalloc(int num_modes, int cutoff, int pure, int dtype, int mode, const void* state,
                              void* out, void* stream);
 

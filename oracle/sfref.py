@@ -40,9 +40,9 @@ _REPO = os.path.dirname(_HERE)
 
 def find_reference():
     """Return the directory holding the ``strawberryfields`` package of the
-    reference: the offline install under ``baseline/_ref`` first, then the
-    read-only source checkout; ``None`` when neither exists."""
-    cands = [os.path.join(_REPO, "baseline", "_ref"), "/root/reference"]
+    reference: ``$SF_REFERENCE_ROOT`` when set, else the offline install under
+    ``baseline/_ref``; ``None`` when neither holds it."""
+    cands = [os.path.join(_REPO, "baseline", "_ref")]
     env = os.environ.get("SF_REFERENCE_ROOT")
     if env:
         cands.insert(0, env)
