@@ -139,6 +139,19 @@ int fock_vacuum(int num_modes, int cutoff, int pure, int dtype, void* state, voi
 int fock_prepare_modes(int num_modes, int cutoff, int dtype, int n_sub, const int* modes,
                        const void* sub, const void* in, void* out, void* workspace, void* stream);
 int64_t fock_prepare_workspace_bytes(int num_modes, int cutoff, int dtype, int n_sub);
+/* out = in (x) |0...0> with `n_new` vacuum modes appended after the
+ * `num_modes` modes of `in` (pure: [D]^(num_modes + n_new); mixed:
+ * interleaved [D]^(2 (num_modes + n_new))); Circuit.alloc,
+ * fockbackend/circuit.py:373-382 (BaseBackend.add_mode, base.py:175). */
+int fock_append_vacuum(int num_modes, int n_new, int cutoff, int pure, int dtype, const void* in, void* out,
+                       void* stream);
+/* out = Tr_modes(rho) for a mixed state: the `n_traced` modes listed in
+ * `modes` (host, distinct, fewer than num_modes) are traced out, the others
+ * keep their order with interleaved axes; FP64 sums.  Circuit.dealloc via
+ * ops.partial_trace, fockbackend/circuit.py:384-391 and ops.py:144
+ * (BaseBackend.del_mode, base.py:186). */
+int fock_partial_trace(int num_modes, int cutoff, int dtype, int n_traced, const int* modes, const void* rho,
+                       void* out, void* stream);
 
 /* ------------------------------------------------------------ readouts (R1-R3)
  * probs: |psi|^2 (pure) or diag(rho) (mixed), D^n doubles

@@ -93,6 +93,38 @@ def _make_fock_gradients():
     return m
 
 
+def _make_symplectic():
+    """``thewalrus.symplectic`` helpers the reference's state tests import
+    (published definitions: a phase-space rotation by theta, the symplectic
+    form, and the reordering between (x1, p1, x2, p2, ...) and
+    (x1, x2, ..., p1, p2, ...) phase-space orderings)."""
+    m = types.ModuleType("thewalrus.symplectic")
+
+    def rotation(theta):
+        c, s = np.cos(theta), np.sin(theta)
+        return np.array([[c, -s], [s, c]])
+
+    def sympmat(n):
+        z, i = np.zeros((n, n)), np.identity(n)
+        return np.block([[z, i], [-i, z]])
+
+    def _xxpp_order(n2):
+        return np.concatenate([np.arange(0, n2, 2), np.arange(1, n2, 2)])
+
+    def xpxp_to_xxpp(S):
+        S = np.asarray(S)
+        ind = _xxpp_order(S.shape[0])
+        return S[ind] if S.ndim == 1 else S[ind][:, ind]
+
+    def xxpp_to_xpxp(S):
+        S = np.asarray(S)
+        ind = np.argsort(_xxpp_order(S.shape[0]))
+        return S[ind] if S.ndim == 1 else S[ind][:, ind]
+
+    m.rotation, m.sympmat, m.xpxp_to_xxpp, m.xxpp_to_xpxp = rotation, sympmat, xpxp_to_xxpp, xxpp_to_xpxp
+    return m
+
+
 # ---------------------------------------------------------------------------
 # permissive stubs for absent modules
 # ---------------------------------------------------------------------------
@@ -165,6 +197,8 @@ class _StubFinder(importlib.abc.MetaPathFinder, importlib.abc.Loader):
     def create_module(self, spec):
         if spec.name == "thewalrus.fock_gradients":
             return _make_fock_gradients()
+        if spec.name == "thewalrus.symplectic":
+            return _make_symplectic()
         mod = _StubModule(spec.name)
         mod.__path__ = []
         return mod

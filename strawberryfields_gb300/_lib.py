@@ -72,6 +72,8 @@ _SIGS = {
     "fock_vacuum": (_i, [_i, _i, _i, _i, _vp, _vp]),
     "fock_prepare_modes": (_i, [_i, _i, _i, _i, _ip, _vp, _vp, _vp, _vp, _vp]),
     "fock_prepare_workspace_bytes": (_i64, [_i, _i, _i, _i]),
+    "fock_append_vacuum": (_i, [_i, _i, _i, _i, _i, _vp, _vp, _vp]),
+    "fock_partial_trace": (_i, [_i, _i, _i, _i, _ip, _vp, _vp, _vp]),
     "fock_probs": (_i, [_i, _i, _i, _i, _vp, _vp, _vp]),
     "fock_marginals": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp]),
     "fock_marginals_workspace_bytes": (_i64, [_i, _i, _i, _i]),

@@ -16,65 +16,49 @@ Extra ``backend_options``: ``dtype`` (``"complex128"``, the reference's
 precision and the default, or ``"complex64"``) and ``device``.
 """
 
-import string
-
 import numpy as np
 import torch
 
 from .circuit import DeviceCircuit
 from .states import FockStateGB300
 
-indices = string.ascii_lowercase
 
-
-class ModeMap:
-    """Map from external mode indices to internal ones; deleted modes map to
-    None (same behaviour as ``ModeMap`` in strawberryfields/backends/base.py:27)."""
+class ModeRegister:
+    """External mode labels of a circuit.  A label stays valid until its mode
+    is deleted; the internal index of a live label is the number of live
+    labels before it, because deleting a mode removes its axes from the
+    state and appending adds axes at the end.  (The reference keeps the same
+    information as an explicit label -> index list, ``ModeMap`` in
+    strawberryfields/backends/base.py:27-115.)"""
 
     def __init__(self, num_subsystems):
-        self._init = num_subsystems
-        self._map = list(range(num_subsystems))
+        self._initial = num_subsystems
+        self._alive = [True] * num_subsystems
 
     def reset(self):
-        self._map = list(range(self._init))
+        self._alive = [True] * self._initial
 
-    def _ok(self, mode):
-        return mode is not None and 0 <= mode < len(self._map)
+    def live(self):
+        """Labels of the modes that exist, in order."""
+        return [m for m, a in enumerate(self._alive) if a]
 
-    def remap(self, modes):
-        if isinstance(modes, int):
-            return self._map[modes]
-        return [self._map[m] for m in modes]
+    def internal(self, modes):
+        """Internal indices of live labels (int or list); ``ValueError`` for
+        labels out of range or deleted."""
+        single = isinstance(modes, (int, np.integer))
+        ms = [modes] if single else list(modes)
+        if not ms or any(not isinstance(m, (int, np.integer)) or not 0 <= m < len(self._alive)
+                         or not self._alive[m] for m in ms):
+            raise ValueError("The specified modes are not valid.")
+        out = [sum(self._alive[:m]) for m in ms]
+        return out[0] if single else out
 
-    def valid(self, modes):
-        if modes is None:
-            return False
-        if isinstance(modes, int):
-            modes = [modes]
-        if len(modes) == 0 or len(modes) > len(self._map):
-            return False
-        return all(self._ok(m) for m in modes)
+    def append(self, n):
+        self._alive += [True] * n
 
-    def show(self):
-        return self._map
-
-    def delete(self, modes):
-        if isinstance(modes, int):
-            modes = [modes]
-        if not self.valid(modes):
-            raise ValueError("Specified modes for deleting are invalid.")
-        new, ctr = [], 0
-        for m in range(len(self._map)):
-            if m in modes or self._map[m] is None:
-                new.append(None)
-            else:
-                new.append(ctr)
-                ctr += 1
-        self._map = new
-
-    def add(self, num_modes):
-        active = len([m for m in self._map if m is not None])
-        self._map += list(range(active, active + num_modes))
+    def remove(self, modes):
+        for m in modes:
+            self._alive[m] = False
 
 
 class FockGB300Backend:
@@ -88,7 +72,7 @@ class FockGB300Backend:
     def __init__(self):
         self._supported = {"mixed_states": True, "fock_basis": True}
         self._init_modes = None
-        self._modemap = None
+        self._modes = None
         self.circuit = None
         self._options = {}
 
@@ -100,16 +84,7 @@ class FockGB300Backend:
 
     # ----------------------------------------------------------------- modes
     def _remap_modes(self, modes):
-        if isinstance(modes, int):
-            modes = [modes]
-            was_int = True
-        else:
-            was_int = False
-        map_ = self._modemap.show()
-        if not self._modemap.valid(modes) or None in [map_[m] for m in modes]:
-            raise ValueError("The specified modes are not valid.")
-        remapped = self._modemap.remap(modes)
-        return remapped[0] if was_int else remapped
+        return self._modes.internal(modes)
 
     def begin_circuit(self, num_subsystems, **kwargs):
         cutoff_dim = kwargs.get("cutoff_dim", None)
@@ -131,20 +106,27 @@ class FockGB300Backend:
         self._init_modes = num_subsystems
         self.circuit = DeviceCircuit(num_subsystems, cutoff_dim, pure, dtype=dtype,
                                      device=self._options["device"])
-        self._modemap = ModeMap(num_subsystems)
+        self._modes = ModeRegister(num_subsystems)
 
     def add_mode(self, n=1, **kwargs):
-        raise NotImplementedError("fock_gb300 does not add modes after begin_circuit")
+        """Append ``n`` vacuum modes (reference fockbackend/backend.py:130)."""
+        self.circuit.alloc(n)
+        self._modes.append(int(n))
 
     def del_mode(self, modes):
-        raise NotImplementedError("fock_gb300 does not delete modes")
+        """Trace out ``modes``; their labels become invalid (reference
+        fockbackend/backend.py:134)."""
+        if isinstance(modes, (int, np.integer)):
+            modes = [modes]
+        self.circuit.dealloc(self._modes.internal(modes))
+        self._modes.remove(modes)
 
     def get_modes(self):
-        return [i for i, j in enumerate(self._modemap._map) if j is not None]
+        return self._modes.live()
 
     def reset(self, pure=True, **kwargs):
         cutoff = kwargs.get("cutoff_dim", self.circuit._trunc)
-        self._modemap.reset()
+        self._modes.reset()
         self.circuit.reset(pure, num_subsystems=self._init_modes, cutoff_dim=cutoff)
 
     def get_cutoff_dim(self):

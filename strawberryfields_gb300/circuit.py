@@ -257,6 +257,51 @@ class DeviceCircuit:
         self._to_mixed()
         self._gate(L.LOSS, T, 0.0, mode)
 
+    # ------------------------------------------------------------------ modes
+    def alloc(self, n=1):
+        """Append ``n`` vacuum modes after the existing ones (reference
+        circuit.py:373-382)."""
+        n = int(n)
+        if n < 1:
+            raise ValueError("Number of modes to add must be positive -- got {}".format(n))
+        if self._num_modes + n > MAX_MODES:
+            raise ValueError("Fock simulator has a maximum of {} modes".format(MAX_MODES))
+        out = self._empty(n=self._num_modes + n)
+        L.call("fock_append_vacuum", self._num_modes, n, self._trunc, int(self._pure), self._dcode,
+               self._state.data_ptr(), out.data_ptr(), self._stream())
+        self._state = out
+        self._num_modes += n
+        self._theta += [0.0] * n
+        self._kappa += [0.0] * n
+
+    def dealloc(self, modes):
+        """Trace out ``modes``; the circuit is left in a mixed state over the
+        remaining modes, in their order (reference circuit.py:384-391)."""
+        modes = sorted({int(m) for m in modes})
+        if not modes:
+            return
+        self._flush()
+        n, D = self._num_modes, self._trunc
+        keep = [m for m in range(n) if m not in modes]
+        if not keep:
+            raise ValueError("Cannot delete every mode of the circuit")
+        if self._pure:
+            # rho_keep = A A^dagger with A = psi as [kept modes, traced modes]
+            # (a plain GEMM), then the interleaved (ket, bra) axis order
+            k = len(keep)
+            a = self._state.permute(keep + modes).reshape(D ** k, -1)
+            rho = (a @ a.conj().T).reshape([D] * (2 * k))
+            perm = [q + s for q in range(k) for s in (0, k)]
+            self._state = rho.permute(perm).contiguous()
+            self._pure = False
+        else:
+            out = self._empty(pure=False, n=len(keep))
+            L.call("fock_partial_trace", n, D, self._dcode, len(modes), ctypes_int_array(modes),
+                   self._state.data_ptr(), out.data_ptr(), self._stream())
+            self._state = out
+        self._num_modes = len(keep)
+        self._clear_pending()
+
     # ------------------------------------------------------------------ states
     def _to_mixed(self):
         if not self._pure:

@@ -8,6 +8,8 @@ states.py:613-663).  ``ket()``/``dm()`` copy to the host as numpy arrays, like
 the reference; ``ket_tensor()`` exposes the device tensor without a copy.
 """
 
+import sys
+
 import numpy as np
 import torch
 
@@ -23,12 +25,18 @@ class FockStateGB300:
         pure (bool): ket ([D]*n) or density matrix ([D]*2n, interleaved axes)
         cutoff_dim (int): Fock cutoff D
         mode_names (Sequence[str]): optional mode names
-        hbar (float): value of hbar for quadrature readouts
+        hbar (float): value of hbar for quadrature readouts (default: the
+            frontend's ``strawberryfields.hbar`` when Strawberry Fields is
+            imported -- the reference's states always take it from there,
+            states.py:53 -- else 2)
     """
 
     EQ_TOLERANCE = 1e-10
 
-    def __init__(self, state_data, num_modes, pure, cutoff_dim, mode_names=None, hbar=2.0):
+    def __init__(self, state_data, num_modes, pure, cutoff_dim, mode_names=None, hbar=None):
+        if hbar is None:
+            sfmod = sys.modules.get("strawberryfields")
+            hbar = float(getattr(sfmod, "hbar", 2.0)) if sfmod is not None else 2.0
         # same argument order as BaseFockState (states.py:489); state_data is
         # a CUDA tensor ([D]*n pure, [D]*2n mixed) or a host array
         if not torch.is_tensor(state_data):

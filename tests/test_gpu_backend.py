@@ -269,6 +269,83 @@ def test_engine_integration(cuda):
 
 
 @pytest.mark.parametrize("pure", [True, False])
+def test_add_and_delete_modes_match_reference_backend(cuda, pure):
+    """add_mode / del_mode / get_modes against the reference's own
+    FockBackend (fockbackend/backend.py:130-139) on the same call sequence:
+    modes appended in the vacuum, deleted modes traced out, labels of the
+    remaining modes unchanged."""
+    from oracle import sfref
+
+    try:
+        sfref.import_strawberryfields()
+    except ImportError:
+        pytest.skip("reference sources not available")
+    from strawberryfields.backends.fockbackend import FockBackend
+    from strawberryfields_gb300 import FockGB300Backend
+
+    D = 5
+    results = []
+    for cls in (FockBackend, FockGB300Backend):
+        b = cls()
+        b.begin_circuit(2, cutoff_dim=D, pure=pure)
+        b.squeeze(0.3, 0.2, 0)
+        b.displacement(0.4, 1.1, 1)
+        b.add_mode(2)
+        b.beamsplitter(0.7, 0.3, 1, 3)
+        b.two_mode_squeeze(0.2, 0.5, 0, 2)
+        b.del_mode([1])
+        b.kerr_interaction(0.1, 3)
+        b.beamsplitter(0.4, 0.9, 0, 3)
+        modes = b.get_modes()
+        b.add_mode(1)
+        b.displacement(0.2, 0.3, 4)
+        b.del_mode(0)
+        results.append((modes, b.get_modes(), b.state().dm(), b.state(modes=[2, 1]).dm()))
+        with pytest.raises(ValueError):
+            b.displacement(0.1, 0.0, 1)  # deleted label
+        with pytest.raises(ValueError):
+            b.del_mode([0])  # deleted already
+    (m_ref, m2_ref, rho_ref, red_ref), (m_got, m2_got, rho_got, red_got) = results
+    assert m_got == m_ref == [0, 2, 3]
+    assert m2_got == m2_ref == [2, 3, 4]
+    assert rho_got.shape == rho_ref.shape
+    assert np.abs(rho_got - rho_ref).max() < TOL
+    assert np.abs(red_got - red_ref).max() < TOL
+
+
+def test_program_with_new_and_del_runs_unchanged(cuda):
+    """A program that creates and deletes modes (ops.New / ops.Del,
+    strawberryfields/ops.py:2376,2423) gives the reference fock backend's
+    state on fock_gb300."""
+    pytest.importorskip("networkx")
+    pytest.importorskip("sympy")
+    from oracle import sfref
+
+    try:
+        sf = sfref.import_strawberryfields()
+    except ImportError:
+        pytest.skip("reference sources not available")
+    from strawberryfields import ops as O
+    from strawberryfields_gb300 import sf_backend
+
+    prog = sf.Program(2)
+    with prog.context as q:
+        O.Sgate(0.25, 0.1) | q[0]
+        O.Dgate(0.3, 0.4) | q[1]
+        (c,) = O.New(1)
+        O.BSgate(0.6, 0.2) | (q[1], c)
+        O.Del | q[0]
+        O.Kgate(0.07) | c
+        O.S2gate(0.1, 0.3) | (q[1], c)
+    states = []
+    for backend in ("fock", sf_backend()):
+        eng = sf.Engine(backend, backend_options={"cutoff_dim": 6})
+        states.append(eng.run(prog).state.dm())
+    assert states[1].shape == states[0].shape == (6,) * 4
+    assert np.abs(states[1] - states[0]).max() < TOL
+
+
+@pytest.mark.parametrize("pure", [True, False])
 def test_homodyne_distribution_and_sample(cuda, pure):
     from strawberryfields_gb300.circuit import DeviceCircuit
 
