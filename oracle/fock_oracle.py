@@ -710,7 +710,8 @@ def adjoint_grads(gates, params, N, D, grad_final, state=None):
         else:
             lo = np.moveaxis(lam, [m1, m2], [0, 1]).reshape(D, D, -1)
             pi_ = np.moveaxis(psi_in, [m1, m2], [0, 1]).reshape(D, D, -1)
-            C = np.einsum("mpr,nqr->mnpq", lo.conj(), pi_)
+            # C[m,n,p,q] = sum_r conj(lo[m,p,r]) pi[n,q,r], as one GEMM
+            C = (lo.conj().reshape(D * D, -1) @ pi_.reshape(D * D, -1).T).reshape(D, D, D, D).transpose(0, 2, 1, 3)
             for j, dU in enumerate(dUs):
                 g[pi + j] += float(np.real(np.sum(C * dU)))
             Uh = np.conj(U).transpose(1, 0, 3, 2)  # [in1, out1, in2, out2] -> acts as U^dagger

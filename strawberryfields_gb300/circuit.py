@@ -262,13 +262,20 @@ class DeviceCircuit:
         """Append ``n`` vacuum modes after the existing ones (reference
         circuit.py:373-382)."""
         n = int(n)
-        if n < 1:
-            raise ValueError("Number of modes to add must be positive -- got {}".format(n))
+        if n < 0:
+            raise ValueError("Number of modes to add must be non-negative -- got {}".format(n))
+        if n == 0:
+            return
         if self._num_modes + n > MAX_MODES:
             raise ValueError("Fock simulator has a maximum of {} modes".format(MAX_MODES))
         out = self._empty(n=self._num_modes + n)
-        L.call("fock_append_vacuum", self._num_modes, n, self._trunc, int(self._pure), self._dcode,
-               self._state.data_ptr(), out.data_ptr(), self._stream())
+        if self._num_modes == 0:
+            # every mode was deleted: the state is the scalar trace left over
+            L.call("fock_vacuum", n, self._trunc, int(self._pure), self._dcode, out.data_ptr(), self._stream())
+            out.mul_(self._state)
+        else:
+            L.call("fock_append_vacuum", self._num_modes, n, self._trunc, int(self._pure), self._dcode,
+                   self._state.data_ptr(), out.data_ptr(), self._stream())
         self._state = out
         self._num_modes += n
         self._theta += [0.0] * n
@@ -284,8 +291,11 @@ class DeviceCircuit:
         n, D = self._num_modes, self._trunc
         keep = [m for m in range(n) if m not in modes]
         if not keep:
-            raise ValueError("Cannot delete every mode of the circuit")
-        if self._pure:
+            # no modes left: what remains is the trace, as a 0-mode mixed state
+            tr = self.probs().sum()
+            self._state = tr.to(self._tdtype).reshape(())
+            self._pure = False
+        elif self._pure:
             # rho_keep = A A^dagger with A = psi as [kept modes, traced modes]
             # (a plain GEMM), then the interleaved (ket, bra) axis order
             k = len(keep)
@@ -366,6 +376,11 @@ class DeviceCircuit:
         self._state = out
 
     def prepare(self, state, mode):
+        """Prepare one mode in ``state``; a mixed circuit receives a
+        single-mode ket as its density matrix (reference circuit.py:489-528)."""
+        state = np.asarray(state)
+        if not self._pure and state.ndim == 1:
+            state = np.outer(state, state.conj())
         self.prepare_multimode(state, [mode] if isinstance(mode, int) else mode)
 
     def prepare_mode_fock(self, n, mode):
@@ -421,6 +436,8 @@ class DeviceCircuit:
 
     def norm(self):
         s, pure = self.get_state()
+        if self._num_modes == 0:
+            return float(s.real.item())
         if pure:
             return float(torch.linalg.vector_norm(s).item())
         return float(self.probs().sum())

@@ -135,6 +135,8 @@ class FockStateGB300:
         return self._probs_tensor().cpu().numpy()
 
     def trace(self, **kwargs):
+        if self._modes == 0:  # every mode deleted: the data is the trace itself
+            return float(self._tensor.real.item())
         return float(self._probs_tensor().sum().item())
 
     def fock_prob(self, n, **kwargs):

@@ -61,3 +61,59 @@ def test_captured_batch_step_matches_eager(cuda):
         for i in range(len(circuits)):
             o0, o1 = cb.param_offsets[i], cb.param_offsets[i + 1]
             assert torch.allclose(grads[o0:o1], g_e[i].reshape(-1), atol=1e-12)
+
+
+def test_config4_sample_matches_oracle_in_captured_step(cuda):
+    """The 4096-circuit workload's own circuits (modes U{2..5}, cutoff
+    U{6..20}, depth U{2..10}, seed 0) in complex64 through the benchmarked
+    path -- structure groups on several streams, checkpointed groups, the
+    whole step captured as one CUDA graph -- against the oracle: two sampled
+    5-mode circuits at cutoff 17-20 and circuits covering every cutoff bucket
+    of the kernels (<= 8, 12, 16, 20), mixed with a group of two circuits of
+    one structure."""
+    import torch
+    from strawberryfields_gb300.batch import CircuitBatch, random_qnn_batch
+    from strawberryfields_gb300.qnn import target_state
+
+    allc, allp = random_qnn_batch(4096, seed=0)
+    pick, seen = [], set()
+    # two 5-mode circuits at cutoff >= 17 (the shallow ones: the oracle's
+    # cost grows with depth), then one circuit per (cutoff bucket, modes)
+    for i, (nm, D, gates, _) in enumerate(allc):
+        if nm == 5 and D >= 17 and len(gates) <= 3 * 43 and len([j for j in pick if allc[j][0] == 5]) < 2:
+            pick.append(i)
+    for i, (nm, D, gates, _) in enumerate(allc):
+        bucket = min(b for b in (8, 12, 16, 20) if D <= b)
+        if nm < 5 and (bucket, nm) not in seen and len(gates) <= 250:
+            seen.add((bucket, nm))
+            pick.append(i)
+    circuits = [allc[i] for i in pick]
+    params = [allp[i] for i in pick]
+    # a second circuit with the first 5-mode circuit's structure: a group of two
+    circuits.append(circuits[0])
+    params.append(np.asarray(params[0]) * 0.9)
+    assert any(nm == 5 and D >= 17 for nm, D, _, _ in circuits)
+    assert {min(b for b in (8, 12, 16, 20) if D <= b) for _, D, _, _ in circuits} == {8, 12, 16, 20}
+
+    cb = CircuitBatch(circuits, dtype=torch.complex64, streams=4, checkpoint_bytes=64 << 20)
+    assert any(g["circ"].checkpoint > 1 for g in cb.groups)
+    assert any(len(g["idx"]) > 1 for g in cb.groups)
+    targets = {}
+    for nm, D, _, _ in circuits:
+        if (nm, D) not in targets:
+            targets[(nm, D)] = torch.as_tensor(target_state(nm, D, 6, seed=nm * 100 + D), device="cuda")
+    pt = [torch.tensor(p, device="cuda") for p in params]
+    step = cb.capture(pt, targets)
+    losses, grads = step(torch.cat(pt))
+    torch.cuda.synchronize()
+    losses = losses.cpu().numpy()
+    grads = grads.cpu().numpy()
+    for i, (nm, D, gates, npar) in enumerate(circuits):
+        t = targets[(nm, D)].cpu().numpy()
+        psi = fo.run_gates(gates, params[i], nm, D)[-1]
+        s = np.vdot(t, psi)
+        assert abs(losses[i] - (1 - abs(s) ** 2)) < 1e-5, (i, nm, D)
+        ref = fo.adjoint_grads(gates, params[i], nm, D, -2 * s * t)
+        got = grads[cb.param_offsets[i]:cb.param_offsets[i + 1]]
+        rel = np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-30)
+        assert rel < 1e-5, (i, nm, D, len(gates), rel)

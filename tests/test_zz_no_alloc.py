@@ -55,8 +55,9 @@ def _largest_cutoff():
 
     x = torch.zeros(1, dtype=torch.complex128, device="cuda")
     out = torch.empty(1, dtype=torch.complex128, device="cuda")
-    # refused on the size check before the state or output is touched
-    rc = L.load().fock_reduced_dm1_noalloc(1, 4096, 1, L.C128, 0, x.data_ptr(), out.data_ptr(), None)
+    # the largest cutoff any kernel accepts (64) is refused on the scratch
+    # size check, before the state or output is touched
+    rc = L.load().fock_reduced_dm1_noalloc(1, 64, 1, L.C128, 0, x.data_ptr(), out.data_ptr(), None)
     assert rc == L.FOCK_ERR_INVALID
     msg = L.last_error()
     assert "too large" in msg
