@@ -19,6 +19,7 @@ timed on a bounded sample of the circuit on all host cores.
 --impl reference runs only that CPU measurement (rank 0; other ranks exit).
 """
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -44,86 +45,112 @@ def _workload():
     return gates, npar, params
 
 
-def _config(extra=None):
-    cfg = {"workload": "cvqnn-adjoint-gradient", "modes": N_MODES, "cutoff": CUTOFF, "layers": LAYERS,
-           "gates": 232, "params": 400, "state": "pure ket 12^6 complex64", "recurrences": "fp64",
-           "loss": "1-|<psi_t|psi>|^2, target total photons <= 6", "l2": "flushed between steps (256 MB write)",
-           "parallelism": "replicas"}
-    if extra:
-        cfg.update(extra)
-    return cfg
+def _config():
+    """The workload, identical in both arms (precision is the line's dtype)."""
+    return {"workload": "cvqnn-adjoint-gradient", "modes": N_MODES, "cutoff": CUTOFF, "layers": LAYERS,
+            "gates": 232, "params": 400, "recurrences": "fp64",
+            "loss": "1-|<psi_t|psi>|^2, target total photons <= 6", "l2": "flushed between steps (256 MB write)",
+            "parallelism": "replicas"}
 
 
 # ---------------------------------------------------------------------------
-# reference CPU implementation (bounded sample, all host cores)
+# reference CPU implementation (bounded samples of the real circuit, all host cores)
 # ---------------------------------------------------------------------------
+CHUNK_GATES = 8
+
+
 def _ref_worker(args):
-    """Time the reference fockbackend Circuit on one sample of each gate kind
-    (runs in a spawned process)."""
+    """Time the reference fockbackend Circuit on one contiguous chunk of the
+    CV-QNN gate list (runs in a spawned process; the state before the chunk
+    is a seeded random ket: the time of an apply does not depend on values)."""
+    chunk, seed = args
     sys.path.insert(0, ROOT)
     os.environ.setdefault("OMP_NUM_THREADS", "1")
     from oracle import sfref
 
-    ops_mod, Circuit = sfref.load_fock_circuit()
-    rng = np.random.default_rng(args)
+    _ops, Circuit = sfref.load_fock_circuit()
+    gates, _npar, params = _workload()
     c = Circuit(N_MODES, CUTOFF, pure=True)
-    # a non-trivial state first (not timed)
-    for m in range(N_MODES):
-        c.squeeze(0.1, 0.2, m)
-    times = {}
-    samples = [("squeeze", lambda: c.squeeze(rng.uniform(0, .3), rng.uniform(0, 6.28), 2)),
-               ("displacement", lambda: c.displacement(rng.uniform(0, .3), rng.uniform(0, 6.28), 3)),
-               ("beamsplitter", lambda: c.beamsplitter(rng.uniform(0, 1.5), rng.uniform(0, 6.28), 2, 3)),
-               ("rotation", lambda: c.phase_shift(rng.uniform(0, 6.28), 1)),
-               ("kerr", lambda: c.kerr_interaction(rng.uniform(0, .05), 4))]
-    for name, fn in samples:
-        t0 = time.perf_counter()
-        fn()
-        times[name] = time.perf_counter() - t0
-    return times
+    rng = np.random.default_rng(seed)
+    psi = rng.normal(size=(CUTOFF,) * N_MODES) + 1j * rng.normal(size=(CUTOFF,) * N_MODES)
+    c._state = psi / np.linalg.norm(psi)
+    calls = {1: lambda p, a, b: c.phase_shift(p[0], a), 2: lambda p, a, b: c.kerr_interaction(p[0], a),
+             3: lambda p, a, b: c.displacement(p[0], p[1], a), 4: lambda p, a, b: c.squeeze(p[0], p[1], a),
+             5: lambda p, a, b: c.beamsplitter(p[0], p[1], a, b)}
+    sel = gates[chunk * CHUNK_GATES:(chunk + 1) * CHUNK_GATES]
+    t0 = time.perf_counter()
+    for kind, m1, m2, pi in sel:
+        calls[kind](params[pi:pi + 2], m1, m2)
+    return chunk, len(sel), time.perf_counter() - t0
 
 
 def reference_cpu(steps, warmup):
     """Grads/s of the reference's CPU path: (2P+1)-forward central differences
-    with the reference Circuit, the 2P+1 forwards spread over all host cores.
-    Each step times one sample of every gate kind in every worker and
-    extrapolates to the 232-gate circuit."""
+    with the reference fock backend's Circuit, the forwards spread over all
+    host cores.  Each step times contiguous chunks of the real 232-gate
+    circuit, one chunk per core concurrently; once every chunk has been timed
+    (two steps on 16 cores) their sum is a full forward."""
     import multiprocessing as mp
 
-    from strawberryfields_gb300.qnn import qnn_gates
-
-    gates, npar = qnn_gates(N_MODES, LAYERS)
-    counts = {"squeeze": 0, "displacement": 0, "beamsplitter": 0, "rotation": 0, "kerr": 0}
-    names = {1: "rotation", 2: "kerr", 3: "displacement", 4: "squeeze", 5: "beamsplitter"}
-    for g in gates:
-        counts[names[g[0]]] += 1
+    gates, npar, _ = _workload()
+    n_chunks = -(-len(gates) // CHUNK_GATES)
     cores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
-    vals = []
-    sample_s = []
+    times = {}
+    walls = []
     with ctx.Pool(cores) as pool:
         for it in range(warmup + steps):
+            jobs = [((it * cores + w) % n_chunks, 1000 * it + w) for w in range(cores)]
             t0 = time.perf_counter()
-            res = pool.map(_ref_worker, [1000 * it + w for w in range(cores)])
+            res = pool.map(_ref_worker, jobs)
             wall = time.perf_counter() - t0
-            # per-worker forward time estimate; all workers ran concurrently
-            fwd = [sum(counts[k] * r[k] for k in counts) for r in res]
-            t_fwd = float(np.mean(fwd))
-            grads_per_s = cores / ((2 * npar + 1) * t_fwd)
-            if it >= warmup:
-                vals.append(grads_per_s)
-                sample_s.append(wall)
+            if it < warmup:
+                continue
+            walls.append(wall)
+            for chunk, ng, dt in res:
+                times.setdefault(chunk, []).append(dt)
+    per_chunk = {c: float(np.median(v)) for c, v in times.items()}
+    if len(per_chunk) == n_chunks:
+        t_fwd = sum(per_chunk.values())
+        how = f"full forward timed: all {n_chunks} chunks of {CHUNK_GATES} gates"
+    else:
+        per_gate = sum(per_chunk.values()) / sum(
+            len(gates[c * CHUNK_GATES:(c + 1) * CHUNK_GATES]) for c in per_chunk)
+        t_fwd = per_gate * len(gates)
+        how = f"{len(per_chunk)} of {n_chunks} chunks timed, scaled by gate count to the 232 gates"
     return {
-        "value": float(np.median(vals)),
+        "value": cores / ((2 * npar + 1) * t_fwd),
         "unit": "grads/s",
         "cores": cores,
         "kind": "reference",
-        "sample": (f"reference fockbackend Circuit (numba absent: its jitted loops run as numpy; thewalrus "
-                   f"matrices from the FP64 restatement), one squeeze/displacement/beamsplitter/rotation/Kerr "
-                   f"on the 12^6 complex128 ket per worker, {cores} concurrent workers, extrapolated to 232 "
-                   f"gates x (2*{npar}+1) central-difference forwards; {np.mean(sample_s):.1f} s per step"),
-        "forward_s_per_worker": t_fwd,
+        "sample": (f"reference fockbackend Circuit on the 12^6 complex128 ket (numba absent: its jitted loops "
+                   f"run as numpy; thewalrus matrices from the FP64 restatement); {how}, one chunk per core "
+                   f"concurrently; gradient = (2*{npar}+1) central-difference forwards; "
+                   f"{np.mean(walls):.1f} s per step"),
+        "forward_s_per_core": t_fwd,
     }
+
+
+def tf_stand_in(cores):
+    """One gradient of the CV-QNN through the torch-autograd restatement of
+    the TF backend's path (oracle/tf_restatement.py), complex64, on the host
+    cores."""
+    import torch
+
+    from oracle import tf_restatement
+    from strawberryfields_gb300.qnn import target_state
+
+    gates, _npar, params = _workload()
+    t = target_state(N_MODES, CUTOFF, TARGET_PHOTONS, TARGET_SEED)
+    torch.set_num_threads(cores)
+    t0 = time.perf_counter()
+    tf_restatement.tf_style_gradient(gates, params, N_MODES, CUTOFF, t)
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": "grads/s", "cores": cores, "kind": "port",
+            "s_per_gradient": dt,
+            "sample": "tf backend GradientTape: unavailable on this box (TensorFlow not installed); this is a "
+                      "torch-autograd restatement of its path (dense complex64 einsum per gate, custom gate-matrix "
+                      "gradients Re sum(dy conj(dU)), tfbackend/ops.py:190-454,688-854), one full gradient"}
 
 
 # ---------------------------------------------------------------------------
@@ -212,12 +239,89 @@ def _autotune(circ, p):
             "plane_ops_by_tile_columns": tiles, "block_ops_by_adjoint_ctas_per_sm": ctas}
 
 
-def gpu_arm(args, rank, world, cpu_base):
-    import ctypes
+def _timed(fn, st, flush, steps, warmup=1):
+    """Median device time (ms) of fn() over ``steps`` runs, L2 flushed before
+    each, CUDA events on stream ``st``."""
+    import torch
 
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ts = []
+    for _ in range(steps):
+        flush.zero_()
+        e0.record(st)
+        fn()
+        e1.record(st)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return float(np.median(ts))
+
+
+def _fidelity_loss(t):
+    import torch
+
+    def loss_fn(psi):
+        dims = tuple(range(psi.dim() - t.dim(), psi.dim()))
+        s = torch.sum(t.conj() * psi, dim=dims)
+        return torch.sum(1 - (s.real ** 2 + s.imag ** 2))
+
+    return loss_fn
+
+
+def _grad_err_vs_fp64(gates, npar, N, D, params, t, g64, dev):
+    """Relative L2 error of a complex64 gradient against the complex128 GPU
+    sweep of the same circuit (the complex128 sweep is pinned to the oracle at
+    <= 1e-10 by tests/test_gpu_configs.py and tests/test_gpu_grad.py)."""
+    import torch
+
+    from strawberryfields_gb300 import CompiledCircuit
+
+    c128 = CompiledCircuit(N, D, gates, npar, dtype=torch.complex128, device=dev)
+    p = torch.as_tensor(params, device=dev, dtype=torch.float64).clone().requires_grad_(True)
+    _fidelity_loss(t.to(torch.complex128))(c128(p)).backward()
+    g128 = p.grad.detach()
+    return float(torch.linalg.vector_norm(g64 - g128) / torch.linalg.vector_norm(g128))
+
+
+def adjoint_vs_fd(N, D, layers, dev, flush, steps, autotune=True):
+    """Adjoint gradients/s of an N-mode cutoff-D CV-QNN (complex64 state, one
+    CUDA graph per step) against the plain GPU forward + central differences
+    ((2P+1) forward sweeps per gradient), with the gradient error against the
+    FP64 sweep."""
+    import torch
+
+    from strawberryfields_gb300 import CompiledCircuit
+    from strawberryfields_gb300.autograd import GraphedGradient
+    from strawberryfields_gb300.qnn import qnn_gates, qnn_params, target_state
+
+    gates, npar = qnn_gates(N, layers)
+    params = qnn_params(gates, npar, PARAM_SEED, r_max=0.3, a_max=0.3, k_max=0.05)
+    circ = CompiledCircuit(N, D, gates, npar, dtype=torch.complex64, device=dev)
+    t = torch.as_tensor(target_state(N, D, TARGET_PHOTONS, TARGET_SEED), device=dev).to(torch.complex64)
+    p = torch.tensor(params, device=dev)
+    if autotune:
+        circ.autotune(p)
+    gg = GraphedGradient(circ, _fidelity_loss(t), p, warmup=1)
+    st = torch.cuda.current_stream(dev)
+    step_ms = _timed(lambda: gg(p), st, flush, steps, warmup=2)
+    g64 = gg(p)[1].clone()
+    fwd_ms = _timed(lambda: circ.forward_states(p, store_all=False), st, flush, steps, warmup=2)
+    grads_s = 1e3 / step_ms
+    fd_s = 1e3 / ((2 * npar + 1) * fwd_ms)
+    return {"workload": f"{N}-mode cutoff-{D} CV-QNN, {layers} layers, {len(gates)} gates, {npar} params",
+            "grads_per_s": grads_s, "ms_per_step": step_ms, "fd_grads_per_s": fd_s,
+            "gpu_forward_ms": fwd_ms, "adjoint_speedup_vs_fd": grads_s / fd_s, "target": ">= 50x",
+            "grad_rel_err_vs_fp64": _grad_err_vs_fp64(gates, npar, N, D, params, t, g64, dev),
+            "err_note": "relative L2 against the complex128 GPU gradient (itself oracle-pinned at <= 1e-10)"}
+
+
+def gpu_arm(args, rank, world, cpu_base):
     import torch
 
     from strawberryfields_gb300 import CompiledCircuit, _lib
+    from strawberryfields_gb300.autograd import GraphedGradient
     from strawberryfields_gb300.qnn import qnn_params as qnn_params_fn
     from strawberryfields_gb300.qnn import target_state
 
@@ -228,12 +332,12 @@ def gpu_arm(args, rank, world, cpu_base):
     t = torch.as_tensor(target_state(N_MODES, CUTOFF, TARGET_PHOTONS, TARGET_SEED), device=dev).to(torch.complex64)
     p_dev = torch.tensor(params, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    loss_fn = _fidelity_loss(t)
+    st = torch.cuda.current_stream(dev)
 
     def step(p):
         p = p.detach().requires_grad_(True)
-        psi = circ(p)
-        s = torch.sum(t.conj() * psi)
-        loss = 1 - (s.real ** 2 + s.imag ** 2)
+        loss = loss_fn(circ(p))
         loss.backward()
         return p.grad, loss
 
@@ -244,13 +348,6 @@ def gpu_arm(args, rank, world, cpu_base):
     # any capture: tuning reallocates the workspace)
     tune = _autotune(circ, p_dev) if not args.no_autotune else None
     lib = _lib.load()
-    # forward + loss + adjoint captured as one CUDA graph (no per-op events
-    # inside the timed graph)
-    from strawberryfields_gb300.autograd import GraphedGradient
-
-    def loss_fn(psi):
-        s = torch.sum(t.conj() * psi)
-        return 1 - (s.real ** 2 + s.imag ** 2)
 
     def run(graphed):
         if graphed is not None:
@@ -259,6 +356,7 @@ def gpu_arm(args, rank, world, cpu_base):
             g, loss = step(p_dev)
         return g
 
+    # forward + loss + adjoint captured as one CUDA graph
     graphed = None
     if not args.eager:
         graphed = GraphedGradient(circ, loss_fn, p_dev, warmup=1)
@@ -269,7 +367,6 @@ def gpu_arm(args, rank, world, cpu_base):
         torch.distributed.barrier()
     clocks = ClockSampler(dev.index)
     clocks.start()
-    st = torch.cuda.current_stream(dev)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     torch.cuda.synchronize()
     wall0 = time.perf_counter()
@@ -286,134 +383,109 @@ def gpu_arm(args, rank, world, cpu_base):
 
     value, my_ms = job_throughput(float(np.sum(step_ms)), args.steps)
     ms_per_step = my_ms / args.steps
-
-    # per-op kernel times: the same step with an event before and after every
-    # op (a separate capture, after the timed region)
-    _lib.check(lib.fock_plan_enable_timing(circ._plan, 1))
-    timed = GraphedGradient(circ, loss_fn, p_dev, warmup=1) if not args.eager else None
+    g64 = run(graphed).clone()
     nops = circ.n_ops
-    fwd_ms = np.zeros(nops, dtype=np.float32)
-    bwd_ms = np.zeros(nops, dtype=np.float32)
-    fbuf = (ctypes.c_float * nops)()
-    bbuf = (ctypes.c_float * nops)()
-    op_steps = max(1, min(args.steps, 5))
-    for k in range(op_steps):
-        flush.zero_()
-        run(timed)
-        torch.cuda.synchronize()
-        _lib.check(lib.fock_plan_op_times(circ._plan, fbuf, bbuf))
-        fwd_ms += np.frombuffer(fbuf, dtype=np.float32)
-        bwd_ms += np.frombuffer(bbuf, dtype=np.float32)
-    _lib.check(lib.fock_plan_enable_timing(circ._plan, 0))
-    del timed
-
-    # per-op kernel roofline (averages over the op-timing steps)
-    fwd_ms /= op_steps
-    bwd_ms /= op_steps
-    ops = circ.ops()
     S = circ.info.state_bytes
     peak, peak_kind = _peaks()
-    groups = {}
-    for k, (kind, m1, m2, nf) in enumerate(ops):
-        if circ.op_config(k)[0] == 1:
-            name = "plane1" if kind == 1 else "plane2"
-        else:
-            name = "dense1" if kind == 1 else "block2"
-        for direction, arr, bytes_per in (("apply", fwd_ms, 2 * S), ("adjoint", bwd_ms, 3 * S)):
-            key = f"{direction}_{name}"
-            gsum = groups.setdefault(key, {"launches": 0, "ms": 0.0, "bytes": 0})
-            gsum["launches"] += 1
-            gsum["ms"] += float(arr[k])
-            gsum["bytes"] += bytes_per
-    kern = {}
-    for key, gsum in groups.items():
-        avg = gsum["ms"] / gsum["launches"]
-        kern[key] = {"launches_per_step": gsum["launches"], "avg_launch_us": 1e3 * avg,
-                     "share_of_sweeps": gsum["ms"] / float(fwd_ms.sum() + bwd_ms.sum()),
-                     "algorithmic_gb_per_launch": gsum["bytes"] / gsum["launches"] / 1e9,
-                     "achieved_gbs": gsum["bytes"] / gsum["launches"] / (avg / 1e3) / 1e9}
-    dom = max(kern, key=lambda k: kern[k]["share_of_sweeps"])
-    traffic = _traffic().get(dom)
-    roof = {"bound": "hbm", "kernel": dom, "achieved": round(kern[dom]["achieved_gbs"], 1), "peak": peak,
-            "unit": "GB/s", "frac": round(kern[dom]["achieved_gbs"] / peak, 4),
-            "traffic": traffic, "peak_source": peak_kind,
-            "algorithmic_bytes_per_launch": kern[dom]["algorithmic_gb_per_launch"] * 1e9}
+
+    # roofline inside the step: the forward sweep alone replayed as a graph of
+    # the same launches (programmatic dependent launch on, L2 flushed before
+    # each replay); the adjoint sweep (adjoint launches, the partial-sum
+    # reduction, parameter gradients) and the loss take the rest of the step
+    fwd_graph_ms = None
+    if not args.eager:
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(st)
+        with torch.cuda.stream(side):
+            circ.forward_states(p_dev)
+        st.wait_stream(side)
+        torch.cuda.synchronize()
+        fg = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(fg):
+            fstates = circ.forward_states(p_dev)
+        fwd_graph_ms = _timed(fg.replay, st, flush, max(args.steps, 5), warmup=2)
+        del fg, fstates
+    sweep_fwd_ms = fwd_graph_ms if fwd_graph_ms is not None else ms_per_step / 3
+    sweep_adj_ms = ms_per_step - sweep_fwd_ms
+    classes = {
+        "apply": {"launches_per_step": nops, "algorithmic_bytes_per_launch": 2 * S, "sweep_ms": sweep_fwd_ms},
+        "adjoint": {"launches_per_step": nops, "algorithmic_bytes_per_launch": 3 * S, "sweep_ms": sweep_adj_ms},
+    }
+    for c in classes.values():
+        c["avg_launch_us"] = 1e3 * c["sweep_ms"] / c["launches_per_step"]
+        c["achieved_gbs"] = c["algorithmic_bytes_per_launch"] / (c["avg_launch_us"] * 1e-6) / 1e9
+        c["share_of_step"] = c["sweep_ms"] / ms_per_step
+    dom = max(classes, key=lambda k: classes[k]["sweep_ms"])
+    roof = {"bound": "hbm", "kernel": f"{dom} sweep ({nops} launches per step)",
+            "achieved": round(classes[dom]["achieved_gbs"], 1), "peak": peak, "unit": "GB/s",
+            "frac": round(classes[dom]["achieved_gbs"] / peak, 4), "traffic": _traffic().get(dom),
+            "peak_source": peak_kind, "algorithmic_bytes_per_launch": classes[dom]["algorithmic_bytes_per_launch"],
+            "timing": "in-step: forward sweep graph replayed alone (same launches, PDL on); adjoint = step - forward",
+            "limiter": "latency/issue: the 23.9 MB state is L2-resident (ncu: no pipe or DRAM saturated)"}
+
+    # per-op kernel times (events between ops, programmatic dependent launch
+    # off: serialised launches) for the per-family breakdown
+    kern = None
+    if not args.eager and not args.quick:
+        _lib.check(lib.fock_plan_enable_timing(circ._plan, 1))
+        timed = GraphedGradient(circ, loss_fn, p_dev, warmup=1)
+        fwd_ms = np.zeros(nops, dtype=np.float32)
+        bwd_ms = np.zeros(nops, dtype=np.float32)
+        fbuf, bbuf = (ctypes.c_float * nops)(), (ctypes.c_float * nops)()
+        op_steps = max(1, min(args.steps, 5))
+        for _ in range(op_steps):
+            flush.zero_()
+            timed(p_dev)
+            torch.cuda.synchronize()
+            _lib.check(lib.fock_plan_op_times(circ._plan, fbuf, bbuf))
+            fwd_ms += np.frombuffer(fbuf, dtype=np.float32)
+            bwd_ms += np.frombuffer(bbuf, dtype=np.float32)
+        _lib.check(lib.fock_plan_enable_timing(circ._plan, 0))
+        del timed
+        fwd_ms /= op_steps
+        bwd_ms /= op_steps
+        groups = {}
+        for k, (kind, m1, m2, nf) in enumerate(circ.ops()):
+            fam = "plane" if circ.op_config(k)[0] == 1 else ("dense" if kind == 1 else "block")
+            name = fam + ("1" if kind == 1 else "2")
+            for direction, arr, bytes_per in (("apply", fwd_ms, 2 * S), ("adjoint", bwd_ms, 3 * S)):
+                gs = groups.setdefault(f"{direction}_{name}", {"launches": 0, "ms": 0.0, "bytes": 0})
+                gs["launches"] += 1
+                gs["ms"] += float(arr[k])
+                gs["bytes"] += bytes_per
+        tot = float(fwd_ms.sum() + bwd_ms.sum())
+        kern = {k: {"launches_per_step": g["launches"], "avg_launch_us": 1e3 * g["ms"] / g["launches"],
+                    "share": g["ms"] / tot, "achieved_gbs": g["bytes"] / (g["ms"] / 1e3) / 1e9}
+                for k, g in groups.items()}
+        kern["note"] = "per-op CUDA events with programmatic dependent launch off (serialised launches)"
 
     # gradient error against the FP64 (complex128) GPU gradient
-    circ128 = CompiledCircuit(N_MODES, CUTOFF, gates, npar, dtype=torch.complex128, device=dev)
-    t128 = t.to(torch.complex128)
-    p = p_dev.detach().clone().requires_grad_(True)
-    psi = circ128(p)
-    s = torch.sum(t128.conj() * psi)
-    (1 - torch.abs(s) ** 2).backward()
-    g128 = p.grad.detach()
-    g64, _ = step(p_dev)
-    grad_err = float(torch.linalg.vector_norm(g64 - g128) / torch.linalg.vector_norm(g128))
-    del circ128, psi
+    grad_err = _grad_err_vs_fp64(gates, npar, N_MODES, CUTOFF, params, t, g64, dev)
 
     # throughput with a batch of parameter sets: B circuits of the same
     # structure per plan (grid.z), one CUDA graph per step
     batched = None
-    if not args.eager and args.batch > 1:
+    if not args.eager and args.batch > 1 and not args.quick:
         B = args.batch
         circ_b = CompiledCircuit(N_MODES, CUTOFF, gates, npar, dtype=torch.complex64, device=dev, batch=B)
         pb = torch.stack([torch.tensor(qnn_params_fn(gates, npar, seed=100 + i), device=dev) for i in range(B)])
         tune_b = _autotune(circ_b, pb) if not args.no_autotune else None
-
-        def loss_b(psi):
-            s = torch.sum(t.conj() * psi, dim=tuple(range(1, psi.dim())))
-            return torch.sum(1 - (s.real ** 2 + s.imag ** 2))
-
-        gb = GraphedGradient(circ_b, loss_b, pb, warmup=1)
-        for _ in range(args.warmup):
-            gb(pb)
-        torch.cuda.synchronize()
-        eb0, eb1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        bt = []
-        for _ in range(args.steps):
-            flush.zero_()
-            eb0.record(st)
-            gb(pb)
-            eb1.record(st)
-            eb1.synchronize()
-            bt.append(eb0.elapsed_time(eb1))
-        ms_b = float(np.median(bt))
-        batched = {"circuits_per_step": B, "ms_per_step": ms_b, "grads_per_s": B * 1e3 / ms_b,
-                   "autotune": tune_b,
+        gb = GraphedGradient(circ_b, loss_fn, pb, warmup=1)
+        ms_b = _timed(lambda: gb(pb), st, flush, args.steps, warmup=args.warmup)
+        batched = {"circuits_per_step": B, "ms_per_step": ms_b, "grads_per_s": B * 1e3 / ms_b, "autotune": tune_b,
                    "note": "B parameter sets of the same circuit in one batched plan (grid.z), gradient of the "
                            "summed loss w.r.t. every set's parameters"}
         del gb, circ_b
 
     # plain GPU forward + central differences
-    for _ in range(3):
-        circ.forward_states(p_dev, store_all=False)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    nrep = 10
-    e0.record(st)
-    for _ in range(nrep):
-        circ.forward_states(p_dev, store_all=False)
-    e1.record(st)
-    e1.synchronize()
-    fwd_s = e0.elapsed_time(e1) / nrep / 1e3
+    fwd_s = _timed(lambda: circ.forward_states(p_dev, store_all=False), st, flush, 10, warmup=3) / 1e3
     fd_grads_per_s = 1.0 / ((2 * npar + 1) * fwd_s)
-
-    def fwd_ms(c, pp, reps=10):
-        for _ in range(3):
-            c.forward_states(pp, store_all=False)
-        torch.cuda.synchronize()
-        e0.record(st)
-        for _ in range(reps):
-            c.forward_states(pp, store_all=False)
-        e1.record(st)
-        e1.synchronize()
-        return e0.elapsed_time(e1) / reps
 
     # the forward configurations: the QNN forward in complex128 too, and the
     # 3-mode cutoff-10 complex128 plain circuit (per mode S and D, BS on
     # (0,1) and (1,2), R and K per mode; seeded parameters)
     c128 = CompiledCircuit(N_MODES, CUTOFF, gates, npar, dtype=torch.complex128, device=dev)
-    q128_ms = fwd_ms(c128, p_dev)
+    q128_ms = _timed(lambda: c128.forward_states(p_dev, store_all=False), st, flush, 10, warmup=3)
     del c128
     g3, np3 = [], 0
     for m in range(3):
@@ -424,24 +496,22 @@ def gpu_arm(args, rank, world, cpu_base):
     for m in range(3):
         g3 += [(_lib.ROTATION, m, -1, np3), (_lib.KERR, m, -1, np3 + 1)]
         np3 += 2
-    rng3 = np.random.default_rng(0)
-    p3 = torch.tensor(rng3.uniform(0, 0.5, np3), device=dev)
+    p3 = torch.tensor(np.random.default_rng(0).uniform(0, 0.5, np3), device=dev)
     c3 = CompiledCircuit(3, 10, g3, np3, dtype=torch.complex128, device=dev)
-    plain3_ms = fwd_ms(c3, p3, 50)
+    plain3_ms = _timed(lambda: c3.forward_states(p3, store_all=False), st, flush, 50, warmup=3)
     del c3
-    S64 = circ.info.state_bytes
     flops = circ.info.flops_fwd  # real flops of one forward (the apply kernels' MACs)
     forward_configs = {
         "qnn6x12_complex64": {"ms": 1e3 * fwd_s, "gates_per_s": len(gates) / fwd_s,
-                              "gbs": 2 * S64 * nops / fwd_s / 1e9, "fp32_tflops": flops / fwd_s / 1e12},
+                              "gbs": 2 * S * nops / fwd_s / 1e9, "fp32_tflops": flops / fwd_s / 1e12},
         "qnn6x12_complex128": {"ms": q128_ms, "gates_per_s": len(gates) / (q128_ms / 1e3),
-                               "gbs": 4 * S64 * nops / (q128_ms / 1e3) / 1e9,
+                               "gbs": 4 * S * nops / (q128_ms / 1e3) / 1e9,
                                "fp64_tflops": flops / (q128_ms / 1e3) / 1e12,
                                "fp64_note": "GB300 FP64 is about 1.25 TFLOP/s nominal: the complex128 sweep is "
                                             "FP64-pipe-bound"},
         "plain3x10_complex128": {"us": 1e3 * plain3_ms, "gates_per_s": len(g3) / (plain3_ms / 1e3),
                                  "circuits_per_s": 1e3 / plain3_ms},
-        "note": "forward sweeps only (matrix build included), states L2-resident, no flush between reps",
+        "note": "forward sweeps only (matrix build included); L2 flushed before each",
     }
 
     # end to end through the public API with host buffers: params H2D,
@@ -449,6 +519,7 @@ def gpu_arm(args, rank, world, cpu_base):
     p_host = torch.tensor(params).pin_memory()
     g_host = torch.empty(npar, dtype=torch.float64).pin_memory()
     l_host = torch.empty(1, dtype=torch.float32).pin_memory()
+
     def e2e_step():
         pd = p_host.to(dev, non_blocking=True)
         if graphed is not None:
@@ -458,52 +529,68 @@ def gpu_arm(args, rank, world, cpu_base):
         g_host.copy_(g, non_blocking=True)
         l_host.copy_(loss.detach().reshape(1), non_blocking=True)
 
-    for _ in range(args.warmup):
-        e2e_step()
-    torch.cuda.synchronize()
-    e0.record(st)
-    for _ in range(args.steps):
-        e2e_step()
-    e1.record(st)
-    e1.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e_ms = _timed(e2e_step, st, flush, args.steps, warmup=args.warmup)
     e2e = {"value": world * 1e3 / e2e_ms, "unit": "grads/s", "h2d_bytes_per_step": npar * 8,
            "d2h_bytes_per_step": npar * 8 + 4, "ms_per_step": e2e_ms}
+
+    exec_mode = "eager" if graphed is None else "one CUDA graph per step"
+    extra = {}
+    if not args.quick:
+        # the other workload configurations at their sizes (fewer steps)
+        extra["config3_adjoint_4x15x8"] = adjoint_vs_fd(4, 15, 8, dev, flush, max(3, min(args.steps, 10)),
+                                                        autotune=not args.no_autotune)
+        del circ, graphed
+        torch.cuda.empty_cache()
+        extra["config4_batched_4096"] = batched_run(args, dev, steps=3, warmup=1, fp64_sample=256)
+        torch.cuda.empty_cache()
+        extra["config5_lossy_dm_4x14"] = lossy_run(dev, steps=2, warmup=1, fp64=args.lossy_fp64)
 
     # ours per step (as the ncu launch list shows): one matrix build (the
     # adjoint sweep reuses the forward sweep's matrices), nops applies, nops
     # adjoints, one reduction of every op's partial sums, parameter gradients
     launches = 2 * nops + 3
+    cpu_fwd = cpu_base.get("forward_s_per_core") if isinstance(cpu_base, dict) else None
     out = {
         "metric": "CV-QNN grads/s (batched adjoint vs plain kernel+FD, <=1e-5 err); HBM % of peak",
         "value": round(value, 3), "unit": "grads/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 state / fp64 recurrences",
         "data": "synthetic seeded CV-QNN parameters and target",
-        "config": _config({"fused_ops": nops, "wall_s_timed": round(wall, 3),
-                           "execution": "eager" if graphed is None else "one CUDA graph per step",
-                           "autotune": tune}),
-        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "kernels": kern,
+        "config": _config(),
+        "run": {"fused_ops": nops, "wall_s_timed": round(wall, 3),
+                "execution": exec_mode, "autotune": tune},
+        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "sweeps": classes, "kernels": kern,
         "grad_rel_err_vs_fp64": grad_err,
+        "grad_err_note": "relative L2 against the complex128 GPU gradient, which tests/test_gpu_configs.py pins "
+                         "to the oracle at <= 1e-10",
         "fd_baseline": {"gpu_forward_ms": 1e3 * fwd_s, "grads_per_s": fd_grads_per_s,
                         "adjoint_speedup": value / world / fd_grads_per_s},
+        "cpu_vs_gpu_forward": ({"reference_forward_s_per_core": cpu_fwd, "gpu_forward_ms": 1e3 * fwd_s,
+                                "ratio_per_forward": cpu_fwd / fwd_s,
+                                "note": "one reference fock forward (complex128, one core) against one GPU "
+                                        "forward sweep (complex64): the speed-up without the algorithm change; "
+                                        "the line's ratio to the reference arm also folds in adjoint vs "
+                                        "(2P+1)-forward central differences"} if cpu_fwd else None),
         "batched_throughput": batched,
         "forward_configs": forward_configs,
         "clocks": clk, "cpu_baseline": cpu_base,
     }
+    out.update(extra)
     return out
 
 
 def single_gate_case(args):
-    """Single-gate kernels on a 7-mode cutoff-12 complex64 ket (287 MB, larger
-    than L2; --modes / --cutoff choose another): forward apply and adjoint of a squeezer on an inner axis and on
-    the last axis, and of a beamsplitter on an inner and on the last adjacent
-    pair.  Each op is its own compiled one-gate circuit, timed with the plan's
-    per-op events (apply = the apply launch; adjoint = the adjoint launch and
-    its partial-sum reduction; the matrix build is outside both).  Bytes per
-    launch are 2 S (apply) and 3 S (adjoint); L2 is flushed before each."""
-    import ctypes
-
+    """Single-gate kernels, each op its own compiled one-gate circuit timed
+    with the plan's per-op events (apply = the apply launch; adjoint = the
+    adjoint launch and its partial-sum reduction; the matrix build is outside
+    both); bytes per launch 2 S (apply) and 3 S (adjoint); L2 flushed before
+    each sweep.  Pure (default): a 7-mode cutoff-12 complex64 ket (287 MB;
+    --modes / --cutoff choose another), a squeezer on an inner axis and on the
+    last axis, a beamsplitter on an inner and on the last adjacent pair.
+    --mixed: the lossy workload's density matrix (4 modes, cutoff 14, 14^8
+    complex64, 11.8 GB): a squeezer on every mode (its ket-side op and its
+    bra-side op), beamsplitters on adjacent pairs, the loss channel on every
+    mode."""
     import torch
 
     from strawberryfields_gb300 import CompiledCircuit
@@ -511,45 +598,59 @@ def single_gate_case(args):
 
     dev = torch.device("cuda", 0)
     lib = _lib.load()
-    N, D = args.modes, args.cutoff
-    cases = {"dense1_inner": [(4, 2, -1, 0)], "dense1_last": [(4, N - 1, -1, 0)],
-             "block2_inner": [(5, 2, 3, 0)], "block2_last": [(5, N - 2, N - 1, 0)]}
+    mixed = args.mixed
+    N, D = (4, 14) if mixed else (args.modes, args.cutoff)
+    if mixed:
+        cases = {f"dense1_m{m}": [(4, m, -1, 0)] for m in range(N)}
+        cases.update({f"block2_m{m}{m + 1}": [(5, m, m + 1, 0)] for m in range(N - 1)})
+        cases.update({f"loss_m{m}": [(9, m, -1, 0)] for m in range(N)})
+    else:
+        cases = {"dense1_inner": [(4, 2, -1, 0)], "dense1_last": [(4, N - 1, -1, 0)],
+                 "block2_inner": [(5, 2, 3, 0)], "block2_last": [(5, N - 2, N - 1, 0)]}
     if args.only:
         cases = {k: v for k, v in cases.items() if k in args.only.split(",")}
-    rng = np.random.default_rng(0)
-    x = torch.as_tensor(rng.normal(size=(D,) * N).astype(np.float32)
-                        + 1j * rng.normal(size=(D,) * N).astype(np.float32), device=dev)
-    x = (x / torch.linalg.vector_norm(x)).to(torch.complex64)
+    naxes = 2 * N if mixed else N
+    g = torch.Generator(device=dev).manual_seed(0)
+    x = torch.view_as_complex(torch.randn((D,) * naxes + (2,), device=dev, generator=g))
+    x = (x / torch.linalg.vector_norm(x)).contiguous()
     lam = x.clone()
     peak, peak_kind = _peaks()
     S = x.numel() * 8
     res = {}
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    fbuf, bbuf = (ctypes.c_float * 1)(), (ctypes.c_float * 1)()
     for name, gates in cases.items():
-        circ = CompiledCircuit(N, D, gates, 2, dtype=torch.complex64, device=dev)
+        circ = CompiledCircuit(N, D, gates, 2, dtype=torch.complex64, device=dev, pure=not mixed)
+        nops = circ.n_ops
+        fbuf, bbuf = (ctypes.c_float * nops)(), (ctypes.c_float * nops)()
         _lib.check(lib.fock_plan_enable_timing(circ._plan, 1))
-        p = torch.tensor([0.3, 0.7], device=dev, dtype=torch.float64)
+        p = torch.tensor([0.3, 0.7] if gates[0][0] != 9 else [0.9, 0.0], device=dev, dtype=torch.float64)
         for _ in range(args.warmup):
             states = circ.forward_states(p, state_in=x)
             circ.backward(p, states, lam, state_in=x)
-        ta, tb = [], []
+            del states
+        ta, tb = [[] for _ in range(nops)], [[] for _ in range(nops)]
         for _ in range(args.steps):
             flush.zero_()
             states = circ.forward_states(p, state_in=x)
             flush.zero_()
             circ.backward(p, states, lam, state_in=x)
             torch.cuda.synchronize(dev)
+            del states
             _lib.check(lib.fock_plan_op_times(circ._plan, fbuf, bbuf))
-            ta.append(fbuf[0])
-            tb.append(bbuf[0])
-        ta_ms, tb_ms = float(np.median(ta)), float(np.median(tb))
-        res[name] = {"apply_us": 1e3 * ta_ms, "apply_gbs": 2 * S / (ta_ms / 1e3) / 1e9,
-                     "adjoint_us": 1e3 * tb_ms, "adjoint_gbs": 3 * S / (tb_ms / 1e3) / 1e9}
-        for k in ("apply_gbs", "adjoint_gbs"):
-            res[name][k.replace("gbs", "frac")] = res[name][k] / peak
-        del circ, states
-    print(json.dumps({"case": "single-gate", "state": f"{D}^{N} complex64 ({S / 1e6:.0f} MB)",
+            for k in range(nops):
+                ta[k].append(fbuf[k])
+                tb[k].append(bbuf[k])
+        for k in range(nops):
+            ta_ms, tb_ms = float(np.median(ta[k])), float(np.median(tb[k]))
+            key = name if nops == 1 else f"{name}_{'ket' if k == 0 else 'bra'}"
+            res[key] = {"apply_us": 1e3 * ta_ms, "apply_gbs": 2 * S / (ta_ms / 1e3) / 1e9,
+                        "adjoint_us": 1e3 * tb_ms, "adjoint_gbs": 3 * S / (tb_ms / 1e3) / 1e9}
+            for q in ("apply_gbs", "adjoint_gbs"):
+                res[key][q.replace("gbs", "frac")] = res[key][q] / peak
+        del circ
+        torch.cuda.empty_cache()
+    print(json.dumps({"case": "single-gate", "state": f"{D}^{naxes} complex64 ({S / 1e6:.0f} MB)"
+                      + (" density matrix" if mixed else " ket"),
                       "note": "kernel time from per-op events: apply = 1 apply launch; adjoint = 1 adjoint "
                               "launch + its partial-sum reduction (median over steps, L2 flushed before each)",
                       "kernels_env": os.environ.get("FOCK_GB300_KERNELS", "default"),
@@ -557,37 +658,34 @@ def single_gate_case(args):
     return 0
 
 
-def lossy_case(args):
-    """Mixed-state lossy gradient: 4-mode cutoff-14 density matrix (14^8
-    complex64 entries, 11.8 GB), 6 CV-QNN layers with a loss channel on every
-    mode per layer; loss = mean photon number of mode 0; forward checkpoints
-    every 2 layers, each 2-layer segment recomputed recursively in the device
-    memory left (a pool of `slots` states).  A step is one forward + one
-    adjoint gradient of all parameters.  Checked by the trace of rho and a
-    central-difference directional derivative (complex64 forward, h = 1e-2)."""
+def _lossy_grad(N, D, layers, dev, dtype, steps, warmup, params=None):
+    """Forward + checkpointed adjoint gradient of the lossy CV-QNN on an
+    N-mode cutoff-D density matrix (loss <n_0>); checkpoints every 2 layers,
+    each segment recomputed recursively in the device memory left.  Returns
+    (gradient, s per gradient, loss, trace, info)."""
     import torch
 
     from strawberryfields_gb300 import CompiledCircuit
     from strawberryfields_gb300.qnn import lossy_qnn_gates, qnn_params
 
-    dev = torch.device("cuda", 0)
-    N, D, layers = 4, 14, 6
     gates, npar = lossy_qnn_gates(N, layers)
-    params = torch.tensor(qnn_params(gates, npar, seed=0), device=dev)
+    if params is None:
+        params = qnn_params(gates, npar, seed=0)
+    p = torch.as_tensor(params, device=dev, dtype=torch.float64)
     # ops per 2 layers (independent of the cutoff)
-    n_ops = CompiledCircuit(N, 2, gates, npar, dtype=torch.complex64, device=dev, pure=False).n_ops
+    n_ops = CompiledCircuit(N, 2, gates, npar, dtype=dtype, device=dev, pure=False).n_ops
     k = 2 * n_ops // layers
-    S = 8 * D ** (2 * N)
+    S = (8 if dtype == torch.complex64 else 16) * D ** (2 * N)
+    torch.cuda.empty_cache()
     free, _ = torch.cuda.mem_get_info(dev)
     n_ckpt = -(-n_ops // k) + 2
     # states: checkpoints + scratch, vacuum input, adjoint pair, pool
     slots = int(min(k - 1, (free - (6 << 30)) // S - n_ckpt - 3))
     if slots < 3:
-        print(json.dumps({"case": "lossy", "unavailable": f"{free / 1e9:.0f} GB free: fewer than 3 recompute slots"}))
-        return 0
-    circ = CompiledCircuit(N, D, gates, npar, dtype=torch.complex64, device=dev, pure=False, checkpoint=k,
+        return None, None, None, None, {"unavailable": f"{free / 1e9:.0f} GB free: fewer than 3 recompute slots"}
+    circ = CompiledCircuit(N, D, gates, npar, dtype=dtype, device=dev, pure=False, checkpoint=k,
                            recompute_slots=slots)
-    nvec = torch.arange(D, device=dev, dtype=torch.float32)
+    nvec = torch.arange(D, device=dev, dtype=torch.float32 if dtype == torch.complex64 else torch.float64)
 
     def diag(rho):
         d = rho
@@ -596,68 +694,97 @@ def lossy_case(args):
         return d  # [D]*N, views only
 
     def step():
-        states = circ.forward_states(params)
+        states = circ.forward_states(p)
         rho = states[circ.final_index()]
-        loss = torch.sum(nvec.reshape(D, 1, 1, 1) * diag(rho).real)
+        loss = torch.sum(nvec.reshape((D,) + (1,) * (N - 1)) * diag(rho).real)
         trace = torch.sum(diag(rho).real)
         g = torch.zeros_like(rho)
-        diag(g).copy_(nvec.reshape(D, 1, 1, 1).expand(D, D, D, D).to(g.dtype))
+        diag(g).copy_(nvec.reshape((D,) + (1,) * (N - 1)).expand((D,) * N).to(g.dtype))
         del rho
-        grads, _ = circ.backward(params, states, g, overwrite_grad=True)
+        grads, _ = circ.backward(p, states, g, overwrite_grad=True)
         del states, g
         return loss, trace, grads
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     times = []
-    for _ in range(args.steps):
+    for _ in range(max(steps, 1)):
         e0.record()
         loss, trace, grads = step()
         e1.record()
         e1.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
-    t = float(np.median(times))
-    # directional derivative against central differences of the forward
-    v = torch.tensor(np.random.default_rng(1).normal(size=npar), device=dev)
-    v /= torch.linalg.vector_norm(v)
-    h = 1e-2
+    info = {"gates": len(gates), "params": npar, "ops": n_ops, "checkpoint_every_ops": k,
+            "recompute_slots": slots, "state_bytes": S}
+    out = (grads.clone(), float(np.median(times)), float(loss), float(trace), info)
+    del circ
+    torch.cuda.empty_cache()
+    return out
 
-    def fwd_loss(pp):
-        st = circ.forward_states(pp, store_all=False)
-        return float(torch.sum(nvec.reshape(D, 1, 1, 1) * diag(st).real))
 
-    fd = (fwd_loss(params + h * v) - fwd_loss(params - h * v)) / (2 * h)
-    ad = float(torch.dot(grads, v))
-    fwd_ops = n_ops
-    print(json.dumps({
-        "case": "lossy", "metric": "mixed-state lossy gradients/s", "value": 1.0 / t, "unit": "grads/s",
-        "s_per_gradient": t, "steps": args.steps, "warmup": args.warmup,
-        "config": {"workload": "4-mode cutoff-14 lossy CV-QNN gradient", "modes": N, "cutoff": D,
-                   "layers": layers, "state": f"density matrix 14^8 complex64 ({S / 1e9:.1f} GB)",
-                   "gates": len(gates), "params": npar, "ops": n_ops, "checkpoint_every_ops": k,
-                   "recompute_slots": slots, "loss": "<n_0>"},
-        "loss": float(loss), "trace": float(trace),
-        "directional_derivative": {"adjoint": ad, "central_difference": fd,
-                                   "rel_err": abs(ad - fd) / max(abs(fd), 1e-30)},
-        "state_bytes": S, "forward_op_bytes": 2 * S * fwd_ops,
-    }))
+def lossy_run(dev, steps, warmup, fp64=False):
+    """The mixed-state lossy workload: 4-mode cutoff-14 density matrix (14^8
+    complex64 entries, 11.8 GB), 6 CV-QNN layers with a loss channel on every
+    mode per layer, loss = <n_0>, checkpointed adjoint gradient.  Its error
+    against FP64: with ``fp64`` the same gradient in complex128 at full size
+    (23.6 GB per state); otherwise the same circuit at cutoff 8 in complex64
+    and complex128 (the full-size complex128 sweep takes minutes)."""
+    import torch
+
+    N, D, layers = 4, 14, 6
+    g64, t, loss, trace, info = _lossy_grad(N, D, layers, dev, torch.complex64, steps, warmup)
+    if g64 is None:
+        return {"case": "lossy", **info}
+    S = info["state_bytes"]
+    out = {"metric": "mixed-state lossy gradients/s", "value": 1.0 / t, "unit": "grads/s", "s_per_gradient": t,
+           "steps": steps, "warmup": warmup,
+           "config": {"workload": "4-mode cutoff-14 lossy CV-QNN gradient", "modes": N, "cutoff": D,
+                      "layers": layers, "state": f"density matrix 14^8 complex64 ({S / 1e9:.1f} GB)",
+                      "loss": "<n_0>", **info},
+           "loss": loss, "trace": trace,
+           "algorithmic_tb_per_gradient": (2 * S * info["ops"] + 3 * S * info["ops"]) / 1e12}
+    if fp64:
+        g128, t128, _, _, info128 = _lossy_grad(N, D, layers, dev, torch.complex128, 1, 0)
+        if g128 is None:
+            out["grad_rel_err_vs_fp64"] = None
+            out["fp64_check"] = info128
+        else:
+            out["grad_rel_err_vs_fp64"] = float(torch.linalg.vector_norm(g64 - g128) / torch.linalg.vector_norm(g128))
+            out["fp64_check"] = {"size": "full (complex128 14^8 density matrix, 23.6 GB per state)",
+                                 "s_per_gradient_complex128": t128, "recompute_slots": info128["recompute_slots"]}
+    else:
+        a, _, _, _, _ = _lossy_grad(N, 8, layers, dev, torch.complex64, 0, 0)
+        b, _, _, _, _ = _lossy_grad(N, 8, layers, dev, torch.complex128, 0, 0)
+        out["grad_rel_err_vs_fp64"] = float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+        out["fp64_check"] = {"size": "the same 6-layer lossy circuit at cutoff 8 (complex64 vs complex128); "
+                                     "full size with bench.py --case lossy --lossy-fp64"}
+    return out
+
+
+def lossy_case(args):
+    import torch
+
+    print(json.dumps({"case": "lossy", **lossy_run(torch.device("cuda", 0), args.steps, args.warmup,
+                                                   fp64=args.lossy_fp64)}))
     return 0
 
 
-def batched_case(args):
+def batched_run(args, dev, steps, warmup, fp64_sample=0):
     """4096 independent CV-QNN circuits, modes U{2..5}, cutoff U{6..20}, depth
     U{2..10} layers (seed 0), complex64: loss and full gradient of every
     circuit per step.  Circuits are grouped by structure into batched compiled
-    circuits spread over CUDA streams; groups whose stored states would exceed
-    8 GB keep checkpoints."""
+    circuits spread over CUDA streams, the whole step one CUDA graph; groups
+    whose stored states would exceed 8 GB keep checkpoints.  With
+    ``fp64_sample`` > 0 that many circuits (seeded sample, every 5-mode
+    cutoff >= 17 circuit of it included) are re-run in complex128 and the
+    graphed complex64 gradients compared with them."""
     import torch
 
     from strawberryfields_gb300.batch import CircuitBatch, random_qnn_batch
     from strawberryfields_gb300.qnn import target_state
 
-    dev = torch.device("cuda", 0)
     n = args.circuits
     t0 = time.perf_counter()
     circuits, params = random_qnn_batch(n, seed=0)
@@ -674,40 +801,62 @@ def batched_case(args):
         t1 = time.perf_counter()
         graphed = cb.capture(pt, targets)
         setup_s += time.perf_counter() - t1
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         graphed(flat) if graphed else cb.value_and_grad(pt, targets)
     torch.cuda.synchronize()
     st = torch.cuda.current_stream(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
-    for _ in range(args.steps):
+    for _ in range(steps):
         if graphed:
             losses, grads = graphed(flat)
         else:
             losses, grads = cb.value_and_grad(pt, targets)
+            grads = torch.cat([g.reshape(-1) for g in grads])
     e1.record(st)
     e1.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
-    # the graphed step against the eager one (same kernels)
-    check = None
-    if graphed:
-        l_e, g_e = cb.value_and_grad(pt, targets)
-        ge = torch.cat([g.reshape(-1) for g in g_e])
-        check = {"max_abs_grad_diff_vs_eager": float(torch.max(torch.abs(ge - grads))),
-                 "max_abs_loss_diff_vs_eager": float(max(abs(float(a) - float(b)) for a, b in zip(l_e, losses)))}
+    ms = e0.elapsed_time(e1) / steps
+    grads = grads.clone()
     stats = cb.stats()
     npar = int(sum(c[3] for c in circuits))
-    out = {"case": "batched", "metric": "circuits/s (forward + adjoint gradient of every circuit)",
-           "value": n / (ms / 1e3), "unit": "circuits/s", "ms_per_step": ms, "steps": args.steps,
-           "warmup": args.warmup, "grads_per_s": n / (ms / 1e3), "params_per_step": npar,
-           "config": {"workload": "4096 heterogeneous CV-QNN circuits", "circuits": n, "modes": "U{2..5}",
+    out = {"metric": "circuits/s (forward + adjoint gradient of every circuit)",
+           "value": n / (ms / 1e3), "unit": "circuits/s", "ms_per_step": ms, "steps": steps,
+           "warmup": warmup, "grads_per_s": n / (ms / 1e3), "params_per_step": npar,
+           "config": {"workload": f"{n} heterogeneous CV-QNN circuits", "circuits": n, "modes": "U{2..5}",
                       "cutoff": "U{6..20}", "depth": "U{2..10} layers", "seed": 0, "dtype": "complex64"},
            "groups": stats["groups"], "fused_ops": stats["ops"],
            "algorithmic_tb_per_step": (stats["bytes_forward"] + stats["bytes_adjoint"]) / 1e12,
            "achieved_gbs": (stats["bytes_forward"] + stats["bytes_adjoint"]) / (ms / 1e3) / 1e9,
-           "setup_s": setup_s, "execution": "eager" if graphed is None else "one CUDA graph per step",
-           "graph_check": check}
-    print(json.dumps(out))
+           "setup_s": setup_s, "execution": "eager" if graphed is None else "one CUDA graph per step"}
+    del graphed, cb
+    torch.cuda.empty_cache()
+    if fp64_sample:
+        rng = np.random.default_rng(1)
+        big = [i for i, c in enumerate(circuits) if c[0] == 5 and c[1] >= 17]
+        idx = sorted(set(rng.choice(n, size=min(fp64_sample, n), replace=False).tolist()) | set(big[:8]))
+        sub = [circuits[i] for i in idx]
+        cb128 = CircuitBatch(sub, dtype=torch.complex128, device=dev, streams=args.streams)
+        _, g128 = cb128.value_and_grad([pt[i] for i in idx], targets)
+        offs = np.concatenate([[0], np.cumsum([c[3] for c in circuits])])
+        errs = []
+        for j, i in enumerate(idx):
+            a = grads[offs[i]:offs[i + 1]]
+            b = g128[j].reshape(-1)
+            errs.append(float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b).clamp_min(1e-300)))
+        out["grad_rel_err_vs_fp64"] = {"max": max(errs), "median": float(np.median(errs)), "circuits": len(idx),
+                                       "note": "graphed complex64 gradients against a complex128 run of a seeded "
+                                               "sample (incl. 5-mode cutoff >= 17 circuits); the complex128 path "
+                                               "is oracle-pinned by tests/test_gpu_batch.py"}
+        del cb128
+        torch.cuda.empty_cache()
+    return out
+
+
+def batched_case(args):
+    import torch
+
+    print(json.dumps({"case": "batched", **batched_run(args, torch.device("cuda", 0), args.steps, args.warmup,
+                                                       fp64_sample=args.fp64_sample)}))
     return 0
 
 
@@ -724,10 +873,18 @@ def main():
     ap.add_argument("--only", default="", help="single-gate case: comma-separated subset of the kernels")
     ap.add_argument("--modes", type=int, default=7, help="single-gate case: modes of the ket")
     ap.add_argument("--cutoff", type=int, default=12, help="single-gate case: cutoff of the ket")
+    ap.add_argument("--mixed", action="store_true",
+                    help="single-gate case: the 4-mode cutoff-14 density matrix of the lossy workload")
     ap.add_argument("--eager", action="store_true", help="no CUDA graph capture")
     ap.add_argument("--no-autotune", action="store_true", help="default kernel selection (no per-op tuning)")
     ap.add_argument("--batch", type=int, default=16,
                     help="gradient case: parameter sets per step of the extra batched-throughput line")
+    ap.add_argument("--quick", action="store_true",
+                    help="gradient case: the headline only (no per-op breakdown, batch line or other configs)")
+    ap.add_argument("--lossy-fp64", action="store_true",
+                    help="lossy workload: check the gradient against complex128 at full size (minutes)")
+    ap.add_argument("--fp64-sample", type=int, default=256,
+                    help="batched case: circuits re-run in complex128 for the error figure (0: none)")
     args = ap.parse_args()
     if args.case == "single-gate":
         return single_gate_case(args)
@@ -746,9 +903,13 @@ def main():
                 "metric": "CV-QNN grads/s (batched adjoint vs plain kernel+FD, <=1e-5 err); HBM % of peak",
                 "value": base["value"], "unit": "grads/s", "n_gpus": args.gpus, "steps": args.steps,
                 "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "c128 (reference precision)", "data": "synthetic seeded CV-QNN parameters",
-                "config": _config({"arm": "reference fockbackend Circuit, central differences"}),
+                "dtype": "c128 state / fp64 matrices (the reference fock backend's only precision)",
+                "data": "synthetic seeded CV-QNN parameters and target",
+                "config": _config(),
+                "run": {"arm": "reference fockbackend Circuit, central differences (the fock backend has no "
+                               "gradient)"},
                 "cpu_baseline": base,
+                "tf_backend_stand_in": tf_stand_in(base["cores"]),
                 "e2e": {"value": base["value"], "unit": "grads/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -756,17 +917,22 @@ def main():
 
     # CPU baseline first: its spawn pool starts before any GPU work
     cpu_base = None
+    tf_base = None
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
-            cpu_base = reference_cpu(1, 0)
+            cpu_base = reference_cpu(2, 0)
         except Exception as e:  # reference sources absent
             cpu_base = {"unavailable": f"{type(e).__name__}: {e}"}
+        if not args.quick:
+            tf_base = tf_stand_in(os.cpu_count() or 1)
     if world > 1:
         import torch
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         torch.distributed.init_process_group("nccl")
     out = gpu_arm(args, rank, world, cpu_base)
+    if tf_base is not None:
+        out["tf_backend_stand_in"] = tf_base
     if rank == 0:
         print(json.dumps(out))
     if world > 1:
