@@ -296,8 +296,10 @@ int fock_plan_op_config(const fock_plan* plan, int op, int* family, int* adj_cta
  * launches.  `grids` (2 ints, or null) receives the CTAs of the persistent
  * forward and backward launches (0 when the plan uses per-op launches); `error` is
  * nonzero when a grid barrier of the last persistent sweep on `workspace`
- * gave up waiting (the outputs are then invalid).  Synchronous: call after
- * the sweep's stream has been synchronised.  No reference counterpart (the
+ * gave up waiting (the outputs are then invalid).  A barrier gives up after
+ * FOCK_GB300_SWEEP_SPIN_LIMIT polls of its generation word (read at plan
+ * creation; default 2^24, about a second); the launch then returns.
+ * Synchronous: call after the sweep's stream has been synchronised.  No reference counterpart (the
  * reference applies one gate per Python call, fockbackend/circuit.py). */
 int fock_plan_sweep_status(const fock_plan* plan, const void* workspace, int* grids, int* error);
 

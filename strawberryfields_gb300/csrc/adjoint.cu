@@ -68,9 +68,14 @@ static int tile_of(int dtype) { return dtype == FOCK_C64 ? 256 : 128; }
 
 static size_t adjoint_smem(int dtype, int D) {
   const int esz = dtype == FOCK_C64 ? 8 : 16;
+  const size_t ms = (ms_slots(dtype, D) + 1) & ~(size_t)1;
+  // cutoffs past the unrolled buckets run adjoint_generic, which stages only
+  // the matrix (the lam / psi tiles of the unrolled body would not fit shared
+  // memory there: about 300 KB at cutoff 60)
+  if (dmax_bucket(D) == 0) return (size_t)esz * ms;
   const int rows = 4 * ((D + 3) / 4);
   // matrix + the lam and psi tiles
-  return (size_t)esz * (((ms_slots(dtype, D) + 1) & ~(size_t)1) + 2 * (size_t)rows * (tile_of(dtype) + 1));
+  return (size_t)esz * (ms + 2 * (size_t)rows * (tile_of(dtype) + 1));
 }
 
 AdjSched make_adj_sched(int dtype, const AxisView& v, int D, int layout, int nb, int ctas_per_sm) {

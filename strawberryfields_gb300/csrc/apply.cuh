@@ -394,7 +394,9 @@ struct SweepSync {
   unsigned* gen;
   int* err;
   unsigned* items;
+  unsigned spin_limit;  // polls of the generation word before a barrier gives up
 };
+#define SWEEP_SPIN_LIMIT_DEFAULT (1u << 24)
 // CTAs per launch that can be co-resident (0: no persistent kernel for D)
 int sweep_grid(int dtype, int D, int backward);
 // adjoint schedule for a persistent sweep: every block's CTAs fit in `grid`

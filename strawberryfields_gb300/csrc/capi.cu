@@ -17,6 +17,10 @@ int fock_set_error(int code, const char* fmt, ...) {
 }
 
 int fock_check_cuda(cudaError_t e, const char* what) {
+  // a failed runtime call also sets the thread's last CUDA error; read it
+  // here so a later launch check does not report this failure again (a
+  // sticky error, after a device fault, stays set regardless)
+  cudaGetLastError();
   return fock_set_error(FOCK_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 

@@ -84,6 +84,7 @@ struct fock_plan {
   // persistent sweeps (small states): grids, tables, sync words, partials
   int persist = 0;
   int g_fwd = 0, g_bwd = 0;
+  unsigned spin_limit = SWEEP_SPIN_LIMIT_DEFAULT;
   size_t o_sweep = 0, o_sync = 0, o_ppart = 0;
   int64_t ppart_entries = 0;
   // optional per-op timing
@@ -419,6 +420,11 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   const char* sw = getenv("FOCK_GB300_SWEEP_MAX_BYTES");
   const int64_t sweep_max = sw ? (int64_t)atoll(sw) : 0;
   const int64_t sbytes = elems * (dtype == FOCK_C64 ? 8 : 16);
+  // FOCK_GB300_SWEEP_SPIN_LIMIT: polls before a grid barrier of the
+  // persistent sweeps gives up (default 2^24; a small value makes a barrier
+  // run out, which the error path's tests use)
+  const char* sl = getenv("FOCK_GB300_SWEEP_SPIN_LIMIT");
+  if (sl) P->spin_limit = (unsigned)strtoul(sl, nullptr, 10);
   if (batch == 1 && sbytes <= sweep_max && dmax_bucket(D) > 0) {
     P->g_fwd = sweep_grid(dtype, D, 0);
     P->g_bwd = sweep_grid(dtype, D, 1);
@@ -626,6 +632,7 @@ static int sweep_sync(fock_plan* P, unsigned char* ws, cudaStream_t st, SweepSyn
   s->gen = w + 1;
   s->err = (int*)(w + 2);
   s->items = w + 4;
+  s->spin_limit = P->spin_limit;
   return FOCK_OK;
 }
 

@@ -12,15 +12,15 @@
 // partial C sums go to a per-op region that the same launch reduces, in a
 // fixed order, after the last op.
 //
-// Every spin has an iteration limit: a barrier that does not complete sets
-// the error flag and the kernel returns (the host reads the flag with
-// fock_plan_sweep_status).  The launch is cooperative, so the runtime refuses
+// Every spin has an iteration limit (SweepSync::spin_limit polls, 2^24 by
+// default, about a second): a barrier that does not complete sets the error
+// flag and the kernel returns (the host reads the flag with
+// fock_plan_sweep_status); every CTA still in the launch then leaves at its
+// next barrier, which sees the flag or runs out its own limit.  The launch is cooperative, so the runtime refuses
 // a grid whose CTAs cannot all be resident instead of letting it wait.
 #include "block_body.cuh"
 
 #include <string.h>
-
-#define SWEEP_SPIN_LIMIT (1u << 24)
 
 // Grid barrier.  Thread 0 of each CTA publishes the CTA's writes (fence after
 // the CTA barrier), arrives, and waits for the generation to change; the
@@ -41,7 +41,7 @@ __device__ __forceinline__ bool sweep_barrier(const SweepSync& s) {
     } else {
       unsigned it = 0;
       while (*vgen == g0) {
-        if (++it > SWEEP_SPIN_LIMIT) {
+        if (++it > s.spin_limit) {
           atomicExch(s.err, 1);
           good = 0;
           break;

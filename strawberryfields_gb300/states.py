@@ -253,19 +253,33 @@ class FockStateGB300:
 
     # ----------------------------------------------------------------- quadratures
     def quad_expectation(self, mode, phi=0, **kwargs):
-        """<x_phi> and Var(x_phi) of one mode (states.py:730)."""
+        """Mean and variance of the rotated quadrature
+        x_phi = x cos(phi) + p sin(phi) = sqrt(hbar/2) (e^{-i phi} a + e^{i phi} a^dagger)
+        of one mode (states.py:730 interface), from ladder-operator moments of
+        the mode's reduced density matrix rho (built on the device):
+        <a> = sum_n sqrt(n) rho[n, n-1], <a^2> = sum_n sqrt(n(n-1)) rho[n, n-2]
+        (and their daggers from the other off-diagonals), and
+        <a a^dagger + a^dagger a> = sum_n (2n + 1) rho[n, n].  These are the
+        moments of the untruncated operators restricted to the cutoff, so the
+        top Fock level contributes (2D - 1) hbar/2 to <x_phi^2>, as in the
+        reference's quadrature operators."""
+        rho = self._rdm1_dev(mode)
         D = self._cutoff
-        a = np.diag(np.sqrt(np.arange(1, D + 5)), 1)
-        x = np.sqrt(self._hbar / 2) * (a + a.T)
-        p = -1j * np.sqrt(self._hbar / 2) * (a - a.T)
-        xphi = np.cos(phi) * x + np.sin(phi) * p
-        xphisq = np.dot(xphi, xphi)
-        xphi = xphi[:D, :D]
-        xphisq = xphisq[:D, :D]
-        rho = self._rdm1(mode)
-        mean = np.trace(np.dot(xphi, rho)).real
-        var = np.trace(np.dot(xphisq, rho)).real - mean ** 2
-        return float(mean), float(var)
+        n = torch.arange(D, dtype=torch.float64, device=rho.device)
+        e1, e2 = np.exp(-1j * phi), np.exp(-2j * phi)
+        a1 = torch.sum(torch.sqrt(n[1:]) * torch.diagonal(rho, offset=-1))
+        a1d = torch.sum(torch.sqrt(n[1:]) * torch.diagonal(rho, offset=1))
+        if D > 2:
+            w2 = torch.sqrt(n[2:] * n[1:-1])
+            a2 = torch.sum(w2 * torch.diagonal(rho, offset=-2))
+            a2d = torch.sum(w2 * torch.diagonal(rho, offset=2))
+        else:
+            a2 = a2d = torch.zeros((), dtype=rho.dtype, device=rho.device)
+        sym = torch.sum((2 * n + 1) * torch.diagonal(rho))
+        h = self._hbar / 2
+        mean = np.sqrt(h) * complex((e1 * a1 + np.conj(e1) * a1d).item()).real
+        second = h * complex((e2 * a2 + np.conj(e2) * a2d + sym).item()).real
+        return float(mean), float(second - mean ** 2)
 
     def wigner(self, mode, xvec, pvec):
         """Discretised Wigner function of one mode (states.py:730): array

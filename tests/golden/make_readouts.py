@@ -9,7 +9,8 @@ then records
 * ``wigner`` (states.py:730) of the first and last mode on a 41 x 37 grid;
 * ``x_quad_values`` / ``p_quad_values`` (states.py:436-475) of mode 0;
 * ``poly_quad_expectation`` (states.py:806) for seeded quadratic, linear and
-  constant coefficients, with and without a quadrature rotation.
+  constant coefficients, with and without a quadrature rotation;
+* ``quad_expectation`` (states.py:787) of every mode at a few rotation angles.
 
 Output: ``readouts/<case>.npz``.
 Usage: python tests/golden/make_readouts.py   (needs the reference sources)
@@ -27,6 +28,7 @@ from oracle import sfref  # noqa: E402
 CASES = ["cfg1_seed0", "mixed_seed0", "mixed_seed1"]
 XVEC = np.linspace(-4.0, 4.0, 41)
 PVEC = np.linspace(-3.5, 3.5, 37)
+QUAD_PHIS = (0.0, np.pi / 4, 1.3, np.pi / 2, 2.9)
 
 
 def poly_cases(N, seed):
@@ -74,11 +76,13 @@ def main():
         ks = np.array([k for _, _, k, _ in pcs])
         phis = np.array([phi for _, _, _, phi in pcs])
         res = np.array([st.poly_quad_expectation(A, d, k, phi=phi) for A, d, k, phi in pcs])
+        qp = np.array(QUAD_PHIS)
+        quad = np.array([[st.quad_expectation(m, phi=phi) for phi in qp] for m in range(N)])
         os.makedirs(os.path.join(HERE, "readouts"), exist_ok=True)
         np.savez_compressed(os.path.join(HERE, "readouts", f"{case}.npz"), source=case, hbar=hbar, xvec=XVEC,
                             pvec=PVEC, wigner_modes=np.array([0, N - 1]), wigner=W, x_quad=xq, p_quad=pq,
                             poly_A=As, poly_A_none=a_none, poly_d=ds, poly_d_none=d_none, poly_k=ks,
-                            poly_phi=phis, poly_mean_var=res)
+                            poly_phi=phis, poly_mean_var=res, quad_phis=qp, quad_mean_var=quad)
         print(case, W.shape, res.shape)
 
 

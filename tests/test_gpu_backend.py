@@ -269,6 +269,35 @@ def test_engine_integration(cuda):
 
 
 @pytest.mark.parametrize("pure", [True, False])
+@pytest.mark.parametrize("gamma", [-0.3, 0.1, 0.45])
+def test_cubic_phase_matches_reference_known_answer(cuda, pure, gamma):
+    """Cubic phase exp(i gamma x^3 / (3 hbar)) (reference fockbackend/ops.py:
+    296-306, built at the cutoff, hbar = 2) on the uniform superposition, on a
+    mode of a 2-mode state, against the known answer of the reference's
+    tests/backend/test_nongaussian_gates.py:32-62 (x = a + a^dagger unscaled,
+    exp(i gamma x^3 / 6)) at 1e-12."""
+    from scipy.linalg import expm
+
+    from strawberryfields_gb300 import FockGB300Backend
+
+    D = 7
+    b = FockGB300Backend()
+    b.begin_circuit(2, cutoff_dim=D, pure=pure)
+    ket = np.ones(D) / np.sqrt(D)
+    b.prepare_ket_state(ket, 1)
+    b.displacement(0.2, 0.4, 0)
+    b.cubic_phase(gamma, 1)
+    a = np.diag(np.sqrt(np.arange(1, D)), 1)
+    x = a + a.T
+    ref1 = expm(1j * gamma * (x @ x @ x) / 6) @ ket
+    ref0 = fo.displacement(0.2, 0.4, D)[:, 0]
+    st = b.state()
+    got = st.dm() if not st.is_pure else np.multiply.outer(st.ket(), st.ket().conj()).transpose(0, 2, 1, 3)
+    ref = np.multiply.outer(np.multiply.outer(ref0, ref0.conj()), np.multiply.outer(ref1, ref1.conj()))
+    assert np.abs(got - ref).max() < TOL
+
+
+@pytest.mark.parametrize("pure", [True, False])
 def test_add_and_delete_modes_match_reference_backend(cuda, pure):
     """add_mode / del_mode / get_modes against the reference's own
     FockBackend (fockbackend/backend.py:130-139) on the same call sequence:

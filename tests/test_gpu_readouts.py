@@ -49,6 +49,15 @@ def test_poly_quad_expectation_matches_reference(cuda, case):
         assert np.allclose(got, r["poly_mean_var"][i], rtol=1e-12, atol=1e-12), (case, i)
 
 
+@pytest.mark.parametrize("case", CASES)
+def test_quad_expectation_matches_reference(cuda, case):
+    st, r, z = _state(case)
+    for m in range(int(z["N"])):
+        for i, phi in enumerate(r["quad_phis"]):
+            got = st.quad_expectation(m, phi=float(phi))
+            assert np.allclose(got, r["quad_mean_var"][m, i], rtol=1e-12, atol=1e-12), (case, m, phi)
+
+
 def test_wigner_complex64_state(cuda):
     st, r, _ = _state(CASES[0], "complex64")
     W = st.wigner(0, r["xvec"], r["pvec"])

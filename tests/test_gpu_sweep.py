@@ -93,3 +93,27 @@ def test_persistent_graph_capture(cuda, persistent):
     assert abs(float(loss) - l_eager) < 1e-6
     assert float(torch.linalg.vector_norm(grad - g_eager)) <= 1e-6 * float(torch.linalg.vector_norm(g_eager))
     assert circ.sweep_status() == (True, 0)
+
+
+def test_barrier_that_runs_out_sets_error_and_returns(cuda, persistent, monkeypatch):
+    """A grid barrier with a spin limit too short for the other CTAs to arrive
+    (FOCK_GB300_SWEEP_SPIN_LIMIT=0: one poll of the generation word) gives up:
+    the kernel sets the error flag and returns, fock_plan_sweep_status reports
+    it, and the device stays usable -- a plan with the default limit then runs
+    the same sweep to the per-op result.  No trap and no unbounded wait: every
+    CTA leaves at its next barrier."""
+    gates, npar = qnn_gates(4, 2)
+    params = torch.tensor(qnn_params(gates, npar, seed=6), device=cuda)
+    monkeypatch.setenv("FOCK_GB300_SWEEP_SPIN_LIMIT", "0")
+    short = CompiledCircuit(4, 8, gates, npar, dtype=torch.complex64, device=cuda)
+    short.forward_states(params, store_all=False)
+    pers, err = short.sweep_status()
+    assert pers and err == 1
+    monkeypatch.delenv("FOCK_GB300_SWEEP_SPIN_LIMIT")
+    good = CompiledCircuit(4, 8, gates, npar, dtype=torch.complex64, device=cuda)
+    psi = good.forward_states(params, store_all=False)
+    pers, err = good.sweep_status()
+    assert pers and err == 0
+    monkeypatch.setenv("FOCK_GB300_SWEEP_MAX_BYTES", "0")
+    ref = CompiledCircuit(4, 8, gates, npar, dtype=torch.complex64, device=cuda)
+    assert torch.equal(psi, ref.forward_states(params, store_all=False))
