@@ -13,7 +13,9 @@ interface ``strawberryfields/backends/base.py:117-626``), so an unchanged
 ``BaseFock`` (required by ``BaseEngine.__init__``, engine.py:74-76); the
 plain :class:`FockGB300Backend` works without Strawberry Fields installed.
 Extra ``backend_options``: ``dtype`` (``"complex128"``, the reference's
-precision and the default, or ``"complex64"``) and ``device``.
+precision and the default, or ``"complex64"``), ``device``, and
+``batch_size`` (B >= 2 copies of the circuit with per-copy gate parameters,
+the TF backend's batch axis: strawberryfields_gb300/batched.py).
 """
 
 import numpy as np
@@ -102,10 +104,17 @@ class FockGB300Backend:
             dtype = "complex64"
         if dtype in (np.complex128, torch.complex128):
             dtype = "complex128"
-        self._options = {"dtype": dtype, "device": kwargs.get("device", None)}
+        batch_size = kwargs.get("batch_size", None)
+        self._options = {"dtype": dtype, "device": kwargs.get("device", None), "batch_size": batch_size}
         self._init_modes = num_subsystems
-        self.circuit = DeviceCircuit(num_subsystems, cutoff_dim, pure, dtype=dtype,
-                                     device=self._options["device"])
+        if batch_size is not None:
+            from .batched import BatchedDeviceCircuit
+
+            self.circuit = BatchedDeviceCircuit(num_subsystems, cutoff_dim, pure, batch_size, dtype=dtype,
+                                                device=self._options["device"])
+        else:
+            self.circuit = DeviceCircuit(num_subsystems, cutoff_dim, pure, dtype=dtype,
+                                         device=self._options["device"])
         self._modes = ModeRegister(num_subsystems)
 
     def add_mode(self, n=1, **kwargs):
@@ -194,7 +203,12 @@ class FockGB300Backend:
         self.circuit.gaussian_gate(S, d, self._remap_modes(list(modes)))
 
     # ----------------------------------------------------------------- measurement
+    def _no_batch(self, what):
+        if self._options.get("batch_size") is not None:
+            raise NotImplementedError(f"{what} is not supported with batch_size")
+
     def measure_fock(self, modes, shots=1, select=None, **kwargs):
+        self._no_batch("measure_fock")
         if shots != 1:
             raise NotImplementedError(
                 "fock_gb300 backend currently does not support shots != 1 for Fock measurement")
@@ -207,6 +221,7 @@ class FockGB300Backend:
             num_bins (int): bins of the sampled distribution (default 100000)
             max (float): the distribution is binned on [-max, max] (default 10)
         """
+        self._no_batch("measure_homodyne")
         if shots != 1:
             raise NotImplementedError("fock backend currently does not support shots != 1 for homodyne measurement")
         return self.circuit.measure_homodyne(phi, self._remap_modes(mode), select=select, **kwargs)
@@ -221,16 +236,38 @@ class FockGB300Backend:
         s, pure = self.circuit.get_state()
         num = self.circuit._num_modes
         cutoff = self.circuit._trunc
+        if self._options.get("batch_size") is not None:
+            return self._batched_state(s, pure, num, cutoff, modes)
         if modes is None:
             names = ["q[{}]".format(i) for i in self.get_modes()]
             return self._state_cls(s, num, pure, cutoff, names)
         if isinstance(modes, int):
             modes = [modes]
+        red = self._reduce(FockStateGB300(s, num, pure, cutoff), modes, num, cutoff)
+        names = ["q[{}]".format(i) for i in np.array(self.get_modes())[modes]]
+        t = torch.as_tensor(np.ascontiguousarray(red), device=s.device).to(s.dtype)
+        return self._state_cls(t, len(modes), False, cutoff, names)
+
+    def _batched_state(self, s, pure, num, cutoff, modes):
+        from .batched import BatchedFockState
+
+        if modes is None:
+            return BatchedFockState(s, num, pure, cutoff, ["q[{}]".format(i) for i in self.get_modes()])
+        single = [self._state_cls(s[b].contiguous(), num, pure, cutoff) for b in range(s.shape[0])]
+        if isinstance(modes, int):
+            modes = [modes]
+        red = torch.stack([torch.as_tensor(np.asarray(
+            FockGB300Backend._reduce(st, modes, num, cutoff)), device=s.device) for st in single]).to(s.dtype)
+        return BatchedFockState(red, len(modes), False, cutoff)
+
+    @staticmethod
+    def _reduce(full, modes, num, cutoff):
+        """Reduced density matrix of ``modes`` (in the given order,
+        interleaved axes) of one state."""
         if len(modes) != len(set(modes)):
             raise ValueError("The specified modes cannot be duplicated.")
         if len(modes) > num:
             raise ValueError("The number of specified modes cannot be larger than the number of subsystems.")
-        full = FockStateGB300(s, num, pure, cutoff)
         srt = sorted(modes)
         red = full.reduced_dm(srt) if srt != list(range(num)) else full.dm()
         red = np.asarray(red).reshape([cutoff] * (2 * len(modes)))
@@ -238,9 +275,7 @@ class FockGB300Backend:
             perm = np.argsort(modes)
             idx = [2 * x + i for x in perm for i in (0, 1)]
             red = np.transpose(red, np.argsort(idx))
-        names = ["q[{}]".format(i) for i in np.array(self.get_modes())[modes]]
-        t = torch.as_tensor(np.ascontiguousarray(red), device=s.device).to(s.dtype)
-        return self._state_cls(t, len(modes), False, cutoff, names)
+        return red
 
 
 _SF_CLASS = None

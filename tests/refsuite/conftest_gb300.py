@@ -77,7 +77,9 @@ def pure(request):
 
 @pytest.fixture(scope="session")
 def batch_size():
-    return None  # the Fock backends have no batch axis in these tests
+    """None, or ``BATCHSIZE`` from the environment (as in the reference's
+    conftest.py:100-114): the backend then runs with its batch_size option."""
+    return int(os.environ["BATCHSIZE"]) if "BATCHSIZE" in os.environ else None
 
 
 @pytest.fixture(params=[pytest.param(BACKEND, marks=pytest.mark.fock)])
