@@ -599,7 +599,7 @@ def single_gate_case(args):
     dev = torch.device("cuda", 0)
     lib = _lib.load()
     mixed = args.mixed
-    N, D = (4, 14) if mixed else (args.modes, args.cutoff)
+    N, D = (4, args.mixed_cutoff) if mixed else (args.modes, args.cutoff)
     if mixed:
         cases = {f"dense1_m{m}": [(4, m, -1, 0)] for m in range(N)}
         cases.update({f"block2_m{m}{m + 1}": [(5, m, m + 1, 0)] for m in range(N - 1)})
@@ -875,6 +875,7 @@ def main():
     ap.add_argument("--cutoff", type=int, default=12, help="single-gate case: cutoff of the ket")
     ap.add_argument("--mixed", action="store_true",
                     help="single-gate case: the 4-mode cutoff-14 density matrix of the lossy workload")
+    ap.add_argument("--mixed-cutoff", type=int, default=14, help="single-gate case with --mixed: the cutoff")
     ap.add_argument("--eager", action="store_true", help="no CUDA graph capture")
     ap.add_argument("--no-autotune", action="store_true", help="default kernel selection (no per-op tuning)")
     ap.add_argument("--batch", type=int, default=16,
