@@ -236,6 +236,15 @@ int fock_plan_get_info(const fock_plan* plan, fock_plan_info* info);
 /* Fused op k: kind code (1 dense single-mode, 2 number-sum block, 3
  * number-difference block), modes, number of gates fused into it. */
 int fock_plan_op(const fock_plan* plan, int k, int* kind, int* mode1, int* mode2, int* n_fused);
+/* Fused tile group of op k: its index (-1 when the op runs on its own), the
+ * group's first op and its number of ops.  A complex64 pure-state plan with
+ * cutoff <= 16 and enough columns groups consecutive ops whose modes lie in
+ * one set of three modes; each group runs as one launch over tiles held in
+ * shared memory (FOCK_GB300_TILE_GROUPS=0 at plan creation turns this off).
+ * Ops are reordered only where they commute (no shared mode), so every
+ * mode's ops keep their order.  No reference counterpart (the reference
+ * applies every gate as its own pass over the state). */
+int fock_plan_op_group(const fock_plan* plan, int k, int* group, int* first, int* count);
 int fock_plan_forward(fock_plan* plan, const double* params, const void* state_in, void* states,
                       int store_every, void* workspace, void* stream);
 int fock_plan_backward(fock_plan* plan, const double* params, const void* state_in,

@@ -85,6 +85,7 @@ _SIGS = {
     "fock_plan_destroy": (None, [_vp]),
     "fock_plan_get_info": (_i, [_vp, ctypes.POINTER(PlanInfo)]),
     "fock_plan_op": (_i, [_vp, _i, _ip, _ip, _ip, _ip]),
+    "fock_plan_op_group": (_i, [_vp, _i, _ip, _ip, _ip]),
     "fock_plan_forward": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp]),
     "fock_plan_backward": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
     "fock_plan_backward_recompute": (_i, [_vp, _vp, _vp, _vp, _i, _vp, _i, _vp, _vp, _vp, _i, _vp, _vp]),

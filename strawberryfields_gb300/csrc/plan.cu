@@ -19,6 +19,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <vector>
 
 namespace {
@@ -49,6 +50,9 @@ struct PlanOp {
   int grid_fwd = 0, grid_adj = 0;
   int adj_ctas = 8;  // adjoint CTAs per SM (block kernels)
   int pl_tc = 0;     // plane-tile columns of a two-mode op (0: the default 32)
+  // fused tile group this op belongs to (-1: none) and the group's chunks
+  int group = -1;
+  int tile_gx = 0;
   // persistent-sweep adjoint schedule and partial-sum region
   AdjSched psched;
   int64_t ppart_off = 0;
@@ -85,6 +89,14 @@ struct fock_plan {
   int persist = 0;
   int g_fwd = 0, g_bwd = 0;
   unsigned spin_limit = SWEEP_SPIN_LIMIT_DEFAULT;
+  // fused three-mode tile groups: ops [k0, k1) on modes m[0] < m[1] < m[2]
+  struct Group {
+    int k0, k1;
+    int m[3];
+  };
+  std::vector<Group> groups;
+  int tile_tc = 0;     // columns per chunk
+  int tile_grid = 0;   // CTAs of a forward group launch
   size_t o_sweep = 0, o_sync = 0, o_ppart = 0;
   int64_t ppart_entries = 0;
   // optional per-op timing
@@ -184,8 +196,8 @@ static void write_red_table(fock_plan* P) {
     red[k].c_off = op.c_off;
     red[k].cpart_off = op.cpart_off;
     red[k].nent = (int)op.nent;
-    red[k].gx = op.plane ? op.grid_adj : op.sched.gx[0];
-    red[k].plane = op.plane;
+    red[k].gx = op.group >= 0 ? op.tile_gx : (op.plane ? op.grid_adj : op.sched.gx[0]);
+    red[k].plane = op.group >= 0 ? 1 : op.plane;
     red[k].layout = op.layout;
   }
 }
@@ -195,14 +207,18 @@ static void write_red_table(fock_plan* P) {
 static void layout_partials(fock_plan* P) {
   int64_t sum = 0, mx = 0;
   for (PlanOp& op : P->ops) {
-    const int64_t part_k = op.plane ? (int64_t)op.grid_adj * op.pg_adj.nent : op.sched.part_entries;
+    const int64_t part_k = op.group >= 0 ? (int64_t)op.tile_gx * op.nent
+                                         : op.plane ? (int64_t)op.grid_adj * op.pg_adj.nent : op.sched.part_entries;
     op.cpart_off = sum;
     sum += part_k;
     mx = std::max(mx, part_k);
   }
   // every op's partials kept until one reduction after the sweep when that
-  // costs at most 512 MiB (about 280 MB for the 6-mode cutoff-12 CV-QNN)
-  P->reduce_at_end = (double)sum * P->batch * sizeof(double2) <= 512.0 * (1 << 20);
+  // costs at most 512 MiB (about 280 MB for the 6-mode cutoff-12 CV-QNN), or
+  // 1.5 GiB for a plan with tile groups (they need it: one partial set per
+  // chunk of columns; 0.8 GB for the same QNN)
+  const double budget = (P->groups.empty() ? 512.0 : 1536.0) * (1 << 20);
+  P->reduce_at_end = (double)sum * P->batch * sizeof(double2) <= budget;
   P->cpart_entries = P->reduce_at_end ? sum : mx;
   size_t o = align256(P->o_cpart + sizeof(double2) * std::max<int64_t>(P->cpart_entries, 1) * P->batch);
   if (P->persist) {
@@ -211,6 +227,99 @@ static void layout_partials(fock_plan* P) {
   }
   P->ws_bytes = o;
   if (P->host) write_red_table(P);
+}
+
+// Group consecutive ops into fused tile groups.  Greedy over a valid order:
+// take the first op not yet placed; among the three-mode sets that contain its
+// modes, pick the one that absorbs the most ready ops (ops whose modes lie in
+// the set and whose predecessors -- earlier ops sharing a mode -- are placed
+// or absorbed), in program order; a set that absorbs one op leaves it a plain
+// op.  The ops are reordered group by group (ops on disjoint modes commute).
+static void form_tile_groups(fock_plan* P) {
+  const int N = P->N, D = P->D, n = (int)P->ops.size();
+  P->groups.clear();
+  if (!P->pure || P->dtype != FOCK_C64 || D > 16 || N < 4 || n < 2) return;
+  double lg = N * log2((double)D);
+  if (lg >= 31.0) return;  // tile offsets are 32-bit
+  int64_t ncols = 1;
+  for (int k = 0; k < N - 3; ++k) ncols *= D;
+  // columns per chunk: 4, or 2 where the adjoint's two tiles would not fit
+  int tc = 4;
+  while (tc > 1 && tile_smem_bytes(D, tc, 1) > 200 * 1024) tc /= 2;
+  if (tile_smem_bytes(D, tc, 1) > 200 * 1024) return;
+  const int64_t nchunks = (ncols + tc - 1) / tc;
+  if (nchunks * P->batch < 2 * fock_num_sms() || nchunks > 65535) return;
+  for (const PlanOp& op : P->ops)
+    if (op.conj || op.owner >= 0) return;
+  // predecessors
+  std::vector<std::vector<int>> pred(n);
+  std::vector<int> last(N, -1);
+  for (int i = 0; i < n; ++i) {
+    const PlanOp& op = P->ops[i];
+    int ms[2] = {op.mode1, op.mode2};
+    for (int q = 0; q < 2; ++q)
+      if (ms[q] >= 0 && last[ms[q]] >= 0) pred[i].push_back(last[ms[q]]);
+    for (int q = 0; q < 2; ++q)
+      if (ms[q] >= 0) last[ms[q]] = i;
+  }
+  std::vector<char> placed(n, 0);
+  std::vector<int> order;
+  std::vector<fock_plan::Group> groups;
+  int first = 0;
+  while ((int)order.size() < n) {
+    while (placed[first]) ++first;
+    const PlanOp& f = P->ops[first];
+    std::vector<std::array<int, 3>> cands;
+    for (int a = 0; a < N; ++a)
+      for (int b = a + 1; b < N; ++b)
+        for (int c = b + 1; c < N; ++c) {
+          const bool has1 = f.mode1 == a || f.mode1 == b || f.mode1 == c;
+          const bool has2 = f.mode2 < 0 || f.mode2 == a || f.mode2 == b || f.mode2 == c;
+          if (has1 && has2) cands.push_back({a, b, c});
+        }
+    std::vector<int> best;
+    std::array<int, 3> best_m = cands[0];
+    for (const auto& m : cands) {
+      std::vector<int> grp;
+      std::vector<char> in(n, 0);
+      for (int i = first; i < n && (int)grp.size() < TL_MAX_OPS; ++i) {
+        if (placed[i]) continue;
+        const PlanOp& op = P->ops[i];
+        auto inset = [&](int md) { return md < 0 || md == m[0] || md == m[1] || md == m[2]; };
+        if (!inset(op.mode1) || !inset(op.mode2)) continue;
+        bool ready = true;
+        for (int pq : pred[i])
+          if (!placed[pq] && !in[pq]) { ready = false; break; }
+        if (!ready) continue;
+        in[i] = 1;
+        grp.push_back(i);
+      }
+      if (grp.size() > best.size()) { best = grp; best_m = m; }
+    }
+    if (best.size() >= 2) {
+      fock_plan::Group g;
+      g.k0 = (int)order.size();
+      g.k1 = g.k0 + (int)best.size();
+      g.m[0] = best_m[0]; g.m[1] = best_m[1]; g.m[2] = best_m[2];
+      groups.push_back(g);
+      for (int i : best) { placed[i] = 1; order.push_back(i); }
+    } else {
+      placed[first] = 1;
+      order.push_back(first);
+    }
+  }
+  if (groups.empty()) return;
+  std::vector<PlanOp> ops;
+  for (int i : order) ops.push_back(P->ops[i]);
+  for (size_t gi = 0; gi < groups.size(); ++gi)
+    for (int k = groups[gi].k0; k < groups[gi].k1; ++k) {
+      ops[k].group = (int)gi;
+      ops[k].tile_gx = (int)nchunks;
+    }
+  P->ops = ops;
+  P->groups = groups;
+  P->tile_tc = tc;
+  P->tile_grid = (int)std::min<int64_t>(nchunks, (int64_t)2 * fock_num_sms());
 }
 
 extern "C" int fock_plan_create(int num_modes, int cutoff, int pure, int dtype, const fock_gate* gates,
@@ -403,6 +512,11 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
     P->ops = ex;
   }
 
+  // fused three-mode tile groups (pure complex64 states, cutoff <= 16, enough
+  // columns to fill the GPU); FOCK_GB300_TILE_GROUPS=0 turns them off
+  const char* tg = getenv("FOCK_GB300_TILE_GROUPS");
+  if (!(tg && strcmp(tg, "0") == 0)) form_tile_groups(P);
+
   // layout of arena / C arena / partials, and tables
   int64_t elems = 1;
   for (int k = 0; k < naxes; ++k) elems *= D;
@@ -425,7 +539,7 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   // run out, which the error path's tests use)
   const char* sl = getenv("FOCK_GB300_SWEEP_SPIN_LIMIT");
   if (sl) P->spin_limit = (unsigned)strtoul(sl, nullptr, 10);
-  if (batch == 1 && sbytes <= sweep_max && dmax_bucket(D) > 0) {
+  if (batch == 1 && sbytes <= sweep_max && dmax_bucket(D) > 0 && P->groups.empty()) {
     P->g_fwd = sweep_grid(dtype, D, 0);
     P->g_bwd = sweep_grid(dtype, D, 1);
     P->persist = P->g_fwd > 0 && P->g_bwd > 0;
@@ -462,6 +576,7 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
       op.grid_fwd = plane_grid(dtype, op.pg_fwd, 0, batch);
       op.grid_adj = plane_grid(dtype, op.pg_adj, 1, batch);
     }
+    if (op.group >= 0) op.plane_ok = 0;  // runs in its tile group
     op.plane = op.plane_ok && (force_plane || plane_preferred(op.layout, op.view));
     if (P->persist) {
       op.psched = make_adj_sched_grid(dtype, op.view, D, op.layout, P->g_bwd);
@@ -598,6 +713,15 @@ extern "C" int fock_plan_get_info(const fock_plan* P, fock_plan_info* info) {
   return FOCK_OK;
 }
 
+extern "C" int fock_plan_op_group(const fock_plan* P, int k, int* group, int* first, int* count) {
+  if (!P || k < 0 || k >= (int)P->ops.size()) return fock_set_error(FOCK_ERR_INVALID, "bad op index");
+  const int gi = P->ops[k].group;
+  if (group) *group = gi;
+  if (first) *first = gi >= 0 ? P->groups[gi].k0 : k;
+  if (count) *count = gi >= 0 ? P->groups[gi].k1 - P->groups[gi].k0 : 1;
+  return FOCK_OK;
+}
+
 extern "C" int fock_plan_op(const fock_plan* P, int k, int* kind, int* mode1, int* mode2, int* n_fused) {
   if (!P || k < 0 || k >= (int)P->ops.size()) return fock_set_error(FOCK_ERR_INVALID, "bad op index");
   const PlanOp& op = P->ops[k];
@@ -657,8 +781,63 @@ static int sweep_ctx(fock_plan* P, unsigned char* ws, cudaStream_t st, SweepCtx*
   return FOCK_OK;
 }
 
+// kernel arguments of ops [k0, k1) of tile group gi (stores and input slots
+// left unset: -1)
+static void tile_arg(const fock_plan* P, int gi, int k0, int k1, TileGroupArg* a) {
+  memset(a, 0, sizeof(*a));
+  const fock_plan::Group& G = P->groups[gi];
+  const int N = P->N, D = P->D;
+  auto stride = [&](int m) {
+    int64_t s = 1;
+    for (int q = m + 1; q < N; ++q) s *= D;
+    return s;
+  };
+  a->D = D;
+  a->T = D * D * D;
+  a->nops = k1 - k0;
+  a->TC = P->tile_tc;
+  for (int i = 0; i < 3; ++i) a->S[i] = stride(G.m[i]);
+  int nr = 0;
+  for (int m = 0; m < N; ++m)
+    if (m != G.m[0] && m != G.m[1] && m != G.m[2]) a->rest_stride[nr++] = stride(m);
+  a->nrest = nr;
+  a->c_fast = G.m[2] != N - 1;
+  a->ncols = 1;
+  for (int q = 0; q < N - 3; ++q) a->ncols *= D;
+  a->nchunks = (a->ncols + a->TC - 1) / a->TC;
+  a->slot_elems = P->state_elems * P->batch;
+  auto ax = [&](int m) { return m == G.m[0] ? 0 : (m == G.m[1] ? 1 : 2); };
+  for (int k = k0; k < k1; ++k) {
+    const PlanOp& op = P->ops[k];
+    TileOp& t = a->ops[k - k0];
+    t.layout = op.layout;
+    if (op.layout == LAYOUT_DENSE) {
+      t.ta = ax(op.mode1);
+      t.tb = -1;
+      t.swap = 0;
+    } else {
+      const int x1 = ax(op.mode1), x2 = ax(op.mode2);
+      t.ta = std::min(x1, x2);
+      t.tb = std::max(x1, x2);
+      t.swap = x1 > x2;
+    }
+    t.nent = (int)op.nent;
+    t.G = tile_group_g(op.layout, D, a->TC);
+    t.m_off = op.m_off;
+    t.store_slot = -1;
+    t.in_slot = -1;
+    t.cpart_off = op.cpart_off;
+  }
+}
+
 static int apply_op(const SweepCtx& c, int k, const void* in, void* out) {
   const PlanOp& op = c.P->ops[k];
+  if (op.group >= 0) {  // one op of a tile group on its own
+    TileGroupArg a;
+    tile_arg(c.P, op.group, k, k + 1, &a);
+    a.ops[0].store_slot = 0;
+    return launch_tile_forward(a, in, out, c.arena, c.P->tile_grid, c.st, c.bt);
+  }
   if (op.plane)
     return launch_plane_apply(c.P->dtype, in, out, op.pg_fwd, op.grid_fwd, c.arena + op.m_off, op_flags(op),
                               c.st, c.bt);
@@ -692,6 +871,24 @@ extern "C" int fock_plan_forward(fock_plan* P, const double* params, const void*
     P->fwd_recorded = 0;
   }
   for (int k = 0; k < n_ops; ++k) {
+    const PlanOp& op = P->ops[k];
+    if (op.group >= 0 && !P->timing && P->groups[op.group].k0 == k) {
+      // a whole tile group in one launch; it writes the outputs the sweep
+      // keeps: every op's (store_every 1), the checkpoints, and the last op's
+      const int k1 = P->groups[op.group].k1;
+      TileGroupArg a;
+      tile_arg(P, op.group, k, k1, &a);
+      for (int j = k; j < k1; ++j) {
+        const bool keep = store_every == 1 || j == k1 - 1 ||
+                          (store_every > 1 && ((j + 1) % store_every == 0 || j == n_ops - 1));
+        a.ops[j - k].store_slot = keep ? out_slot(j, n_ops, store_every) : -1;
+      }
+      c.bt.pdl = k > 0;
+      if ((rc = launch_tile_forward(a, cur, states, c.arena, P->tile_grid, st, c.bt))) return rc;
+      cur = (char*)states + out_slot(k1 - 1, n_ops, store_every) * c.sb;
+      k = k1 - 1;
+      continue;
+    }
     void* dst = (char*)states + out_slot(k, n_ops, store_every) * c.sb;
     if (P->timing && (rc = record_event(P->ev_fwd[k], st))) return rc;
     // the first op follows the matrix build in plain stream order; later ops
@@ -737,7 +934,16 @@ static int adjoint_op(BwdCtx& b, int k, const void* psi_in) {
   if (P->timing && (rc = record_event(P->ev_bwd[k + 1], st))) return rc;
   double2* cout = (double2*)(b.ws + P->o_carena) + op.c_off;
   double2* part = b.cpart + (P->reduce_at_end ? op.cpart_off : 0);
-  if (op.plane) {
+  if (op.group >= 0) {  // one op of a tile group on its own
+    TileGroupArg a;
+    tile_arg(P, op.group, k, k + 1, &a);
+    a.ops[0].cpart_off = 0;
+    rc = launch_tile_adjoint(a, psi_in, psi_in, b.lam, b.other, b.c.arena, part, st, b.c.bt);
+    if (rc) return rc;
+    if (!P->reduce_at_end)
+      rc = launch_reduce_partials(part, op.tile_gx, op.nent, cout, st, P->batch, P->cpart_entries,
+                                  P->carena_entries, b.pdl);
+  } else if (op.plane) {
     rc = launch_plane_adjoint(P->dtype, psi_in, b.lam, b.other, op.pg_adj, op.grid_adj, b.c.arena + op.m_off,
                               op_flags(op), part, st, b.c.bt);
     if (rc) return rc;
@@ -885,8 +1091,22 @@ extern "C" int fock_plan_backward_recompute(fock_plan* P, const double* params, 
   b.pdl = !P->timing;
   b.c.bt.pdl = 0;
   if (K == 1) {
-    for (int k = n_ops - 1; k >= 0; --k)
+    for (int k = n_ops - 1; k >= 0; --k) {
+      const PlanOp& op = P->ops[k];
+      if (op.group >= 0 && !P->timing && P->reduce_at_end && P->groups[op.group].k1 - 1 == k) {
+        // a whole tile group in one launch, lam kept in shared memory
+        const int k0 = P->groups[op.group].k0;
+        TileGroupArg a;
+        tile_arg(P, op.group, k0, k + 1, &a);
+        for (int j = k0; j <= k; ++j) a.ops[j - k0].in_slot = j - 1;  // -1: state_in
+        if ((rc = launch_tile_adjoint(a, state_in, states, b.lam, b.other, c.arena, b.cpart, st, b.c.bt))) return rc;
+        b.c.bt.pdl = b.pdl;
+        std::swap(b.lam, b.other);
+        k = k0;
+        continue;
+      }
       if ((rc = adjoint_op(b, k, k == 0 ? state_in : (const char*)states + (int64_t)(k - 1) * c.sb))) return rc;
+    }
   } else {
     std::vector<void*> pool;
     for (int i = seg_slots - 1; i >= 0; --i) pool.push_back((char*)seg + (int64_t)i * c.sb);

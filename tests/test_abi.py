@@ -280,3 +280,72 @@ def test_autotune_selection_logic(monkeypatch):
     c = Fake(penalty=5.0)  # the CTA picks lose on the whole step: keep densities, take the tile
     cfgs, before, after = c.autotune(None, ctas=(4, 8, 16), tiles=(32, 24))
     assert cfgs == [(0, 8, 256), (1, 8, 24), (0, 8, 32)] and after < before
+
+
+def _plan_ops(lib, N, D, gates, npar, batch=1, dtype=0):
+    from strawberryfields_gb300 import _lib as L
+
+    arr = (L.FockGate * len(gates))()
+    for i, g in enumerate(gates):
+        arr[i].kind, arr[i].mode1, arr[i].mode2, arr[i].pidx = g
+    plan = ctypes.c_void_p()
+    L.check(lib.fock_plan_create_batch(N, D, 1, dtype, arr, len(gates), npar, batch, ctypes.byref(plan)))
+    info = L.PlanInfo()
+    L.check(lib.fock_plan_get_info(plan, ctypes.byref(info)))
+    ops = []
+    for k in range(info.n_ops):
+        a, b, c, d = (ctypes.c_int() for _ in range(4))
+        L.check(lib.fock_plan_op(plan, k, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d)))
+        g, f, n = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        L.check(lib.fock_plan_op_group(plan, k, ctypes.byref(g), ctypes.byref(f), ctypes.byref(n)))
+        ops.append((a.value, b.value, c.value, d.value, g.value, f.value, n.value))
+    lib.fock_plan_destroy(plan)
+    return ops
+
+
+@pytest.mark.parametrize("N,D,layers,batch", [(6, 12, 4, 1), (6, 8, 3, 4), (7, 6, 2, 1), (5, 12, 2, 16)])
+def test_tile_groups_keep_every_modes_order(lib, monkeypatch, N, D, layers, batch):
+    """Fused tile groups (fock_plan_op_group): every op in exactly one group
+    or on its own, each group's ops consecutive and within three modes, and
+    the ops touching any one mode in the same order as without groups (ops
+    are only reordered where they commute)."""
+    from strawberryfields_gb300.qnn import qnn_gates
+
+    gates, npar = qnn_gates(N, layers)
+    monkeypatch.setenv("FOCK_GB300_TILE_GROUPS", "0")
+    plain = _plan_ops(lib, N, D, gates, npar, batch)
+    assert all(o[4] == -1 for o in plain)
+    monkeypatch.delenv("FOCK_GB300_TILE_GROUPS")
+    grouped = _plan_ops(lib, N, D, gates, npar, batch)
+    assert len(grouped) == len(plain)
+    assert any(o[4] >= 0 for o in grouped)
+    for m in range(N):
+        seq_p = [o[:4] for o in plain if m in (o[1], o[2])]
+        seq_g = [o[:4] for o in grouped if m in (o[1], o[2])]
+        assert seq_p == seq_g, m
+    k = 0
+    while k < len(grouped):
+        g, first, count = grouped[k][4:]
+        assert first == k
+        if g < 0:
+            assert count == 1
+        else:
+            modes = set()
+            for j in range(k, k + count):
+                assert grouped[j][4] == g
+                modes |= {grouped[j][1]} | ({grouped[j][2]} if grouped[j][2] >= 0 else set())
+            assert len(modes) <= 3
+            assert count >= 2
+        k += count
+
+
+def test_tile_groups_only_where_they_apply(lib):
+    """No groups for complex128, density matrices, cutoffs above 16 or too few
+    columns (4 modes at cutoff 15: 15 columns)."""
+    from strawberryfields_gb300.qnn import qnn_gates
+
+    g6, n6 = qnn_gates(6, 1)
+    assert all(o[4] == -1 for o in _plan_ops(lib, 6, 12, g6, n6, dtype=1))
+    assert all(o[4] == -1 for o in _plan_ops(lib, 6, 17, g6, n6))
+    g4, n4 = qnn_gates(4, 2)
+    assert all(o[4] == -1 for o in _plan_ops(lib, 4, 15, g4, n4))
