@@ -309,6 +309,13 @@ static void form_tile_groups(fock_plan* P) {
     }
   }
   if (groups.empty()) return;
+  // the adjoint writes one partial C per chunk of columns and op: keep them
+  // within the one-reduction budget (else the per-op path is cheaper)
+  double part = 0.0;
+  for (const fock_plan::Group& g : groups)
+    for (int k = g.k0; k < g.k1; ++k)
+      part += (double)nchunks * layout_entries(P->ops[order[k]].layout, D) * P->batch * sizeof(double2);
+  if (part > 1536.0 * (1 << 20)) return;
   std::vector<PlanOp> ops;
   for (int i : order) ops.push_back(P->ops[i]);
   for (size_t gi = 0; gi < groups.size(); ++gi)
@@ -319,7 +326,10 @@ static void form_tile_groups(fock_plan* P) {
   P->ops = ops;
   P->groups = groups;
   P->tile_tc = tc;
-  P->tile_grid = (int)std::min<int64_t>(nchunks, (int64_t)2 * fock_num_sms());
+  // forward CTAs: every chunk in one wave when the resident CTAs allow it
+  // (shared memory bounds the CTAs per SM; registers allow 4)
+  const int per_sm = std::max(1, std::min(4, (int)((227 * 1024) / tile_smem_bytes(D, tc, 0))));
+  P->tile_grid = (int)std::min<int64_t>(nchunks, (int64_t)per_sm * fock_num_sms());
 }
 
 extern "C" int fock_plan_create(int num_modes, int cutoff, int pure, int dtype, const fock_gate* gates,
