@@ -53,16 +53,15 @@ class BatchedDeviceCircuit:
     def _each(self, fn):
         """Run fn(circuit_of_copy_b, b) on every copy and stack the results."""
         outs = []
-        pure = self._pure
+        pure, num = self._pure, self._num_modes
         for b in range(self.batch_size):
             dc = self._slice_circuit(b)
             fn(dc, b)
             dc._flush()
             outs.append(dc._state)
-            pure = dc._pure
-            self._num_modes = dc._num_modes
+            pure, num = dc._pure, dc._num_modes
         self._state = torch.stack(outs)
-        self._pure = pure
+        self._pure, self._num_modes = pure, num
 
     def _param(self, v):
         """A gate argument as B float64 values (a scalar is broadcast)."""
@@ -198,6 +197,19 @@ class BatchedFockState:
         self._hbar = self._states[0].hbar
 
     batched = True
+
+    @property
+    def data(self):
+        """The batched state as a host array ([B, D, ...])."""
+        return self._data.cpu().numpy()
+
+    @property
+    def mode_names(self):
+        return self._states[0].mode_names
+
+    @property
+    def mode_indices(self):
+        return self._states[0].mode_indices
 
     @property
     def num_modes(self):
