@@ -408,9 +408,9 @@ int launch_sweep_backward(int dtype, int D, const SweepOp* ops, int n_ops, const
                           int64_t slot_elems, void* lam_a, void* lam_b, const double2* arena, double2* cpart,
                           double2* carena, int64_t carena_entries, SweepSync sync, int grid, cudaStream_t st);
 
-// Fused op groups on a three-mode tile (tile.cu): pure complex64 states,
-// cutoff <= 16.  Tile axes 0 < 1 < 2 are the group's modes in increasing
-// order; the other modes index the columns.
+// Fused op groups of the forward sweep on a three-mode tile (tile.cu): pure
+// complex64 states, cutoff <= 16.  Tile axes 0 < 1 < 2 are the group's modes
+// in increasing order; the other modes index the columns.
 #define TL_THREADS 256
 #define TL_MAX_OPS 16
 #define TL_MAX_REST 32
@@ -418,29 +418,20 @@ struct TileOp {
   int layout;          // LAYOUT_DENSE / SUM / DIFF
   int ta, tb;          // tile axes (ta < tb; tb = -1 for one-mode ops)
   int swap;            // stored matrix orientation is (tb, ta)
-  int nent;            // C entries (stored order)
-  int G;               // fibre groups of the adjoint's C pass
   int64_t m_off;       // matrix in the arena
-  int64_t store_slot;  // forward: slot that receives this op's output (-1: none)
-  int64_t in_slot;     // adjoint: slot of this op's input (-1: the sweep's input state)
-  int64_t cpart_off;   // adjoint: partial sums, CTA x at cpart_off + x * nent
+  int64_t store_slot;  // slot that receives this op's output (-1: none)
 };
 struct TileGroupArg {
-  int D, T, nops, nrest, TC, c_fast;
-  int64_t S[3];                     // global strides of the tile modes
+  int D, T, nops, nrest, TC, lgTC, c_fast;
+  int64_t S[3];                      // global strides of the tile modes
   int64_t rest_stride[TL_MAX_REST];  // global strides of the other modes, slowest first
-  int64_t ncols, nchunks;           // columns, chunks of TC columns
-  int64_t slot_elems;               // elements of one stored-state slot (whole batch)
+  int64_t ncols, nchunks;            // columns, chunks of TC columns
+  int64_t slot_elems;                // elements of one stored-state slot (whole batch)
   TileOp ops[TL_MAX_OPS];
 };
-size_t tile_smem_bytes(int D, int TC, int adjoint);
-int tile_group_g(int layout, int D, int TC);
+size_t tile_smem_bytes(int D, int TC);
 int launch_tile_forward(const TileGroupArg& g, const void* in, void* states, const double2* arena, int grid,
                         cudaStream_t st, const BatchArg& bt);
-// one CTA per chunk (grid = g.nchunks); partials of CTA x of op k at
-// cpart + ops[k].cpart_off + x * ops[k].nent
-int launch_tile_adjoint(const TileGroupArg& g, const void* state_in, const void* states, const void* lam_out,
-                        void* lam_in, const double2* arena, double2* cpart, cudaStream_t st, const BatchArg& bt);
 
 // reduced density matrix pieces (capi.cu)
 int launch_rdm_mixed(int dtype, const void* state, int num_modes, int D, int mode, int64_t ntr, int chunks,

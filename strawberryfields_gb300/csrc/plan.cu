@@ -50,9 +50,8 @@ struct PlanOp {
   int grid_fwd = 0, grid_adj = 0;
   int adj_ctas = 8;  // adjoint CTAs per SM (block kernels)
   int pl_tc = 0;     // plane-tile columns of a two-mode op (0: the default 32)
-  // fused tile group this op belongs to (-1: none) and the group's chunks
+  // fused tile group of the forward sweep this op belongs to (-1: none)
   int group = -1;
-  int tile_gx = 0;
   // persistent-sweep adjoint schedule and partial-sum region
   AdjSched psched;
   int64_t ppart_off = 0;
@@ -196,8 +195,8 @@ static void write_red_table(fock_plan* P) {
     red[k].c_off = op.c_off;
     red[k].cpart_off = op.cpart_off;
     red[k].nent = (int)op.nent;
-    red[k].gx = op.group >= 0 ? op.tile_gx : (op.plane ? op.grid_adj : op.sched.gx[0]);
-    red[k].plane = op.group >= 0 ? 1 : op.plane;
+    red[k].gx = op.plane ? op.grid_adj : op.sched.gx[0];
+    red[k].plane = op.plane;
     red[k].layout = op.layout;
   }
 }
@@ -207,18 +206,14 @@ static void write_red_table(fock_plan* P) {
 static void layout_partials(fock_plan* P) {
   int64_t sum = 0, mx = 0;
   for (PlanOp& op : P->ops) {
-    const int64_t part_k = op.group >= 0 ? (int64_t)op.tile_gx * op.nent
-                                         : op.plane ? (int64_t)op.grid_adj * op.pg_adj.nent : op.sched.part_entries;
+    const int64_t part_k = op.plane ? (int64_t)op.grid_adj * op.pg_adj.nent : op.sched.part_entries;
     op.cpart_off = sum;
     sum += part_k;
     mx = std::max(mx, part_k);
   }
   // every op's partials kept until one reduction after the sweep when that
-  // costs at most 512 MiB (about 280 MB for the 6-mode cutoff-12 CV-QNN), or
-  // 1.5 GiB for a plan with tile groups (they need it: one partial set per
-  // chunk of columns; 0.8 GB for the same QNN)
-  const double budget = (P->groups.empty() ? 512.0 : 1536.0) * (1 << 20);
-  P->reduce_at_end = (double)sum * P->batch * sizeof(double2) <= budget;
+  // costs at most 512 MiB (about 280 MB for the 6-mode cutoff-12 CV-QNN)
+  P->reduce_at_end = (double)sum * P->batch * sizeof(double2) <= 512.0 * (1 << 20);
   P->cpart_entries = P->reduce_at_end ? sum : mx;
   size_t o = align256(P->o_cpart + sizeof(double2) * std::max<int64_t>(P->cpart_entries, 1) * P->batch);
   if (P->persist) {
@@ -229,7 +224,8 @@ static void layout_partials(fock_plan* P) {
   if (P->host) write_red_table(P);
 }
 
-// Group consecutive ops into fused tile groups.  Greedy over a valid order:
+// Group consecutive ops into fused tile groups of the forward sweep.  Greedy
+// over a valid order:
 // take the first op not yet placed; among the three-mode sets that contain its
 // modes, pick the one that absorbs the most ready ops (ops whose modes lie in
 // the set and whose predecessors -- earlier ops sharing a mode -- are placed
@@ -243,12 +239,11 @@ static void form_tile_groups(fock_plan* P) {
   if (lg >= 31.0) return;  // tile offsets are 32-bit
   int64_t ncols = 1;
   for (int k = 0; k < N - 3; ++k) ncols *= D;
-  // columns per chunk: 4, or 2 where the adjoint's two tiles would not fit
+  // columns per chunk: 4, or fewer where two CTAs per SM would not fit
   int tc = 4;
-  while (tc > 1 && tile_smem_bytes(D, tc, 1) > 200 * 1024) tc /= 2;
-  if (tile_smem_bytes(D, tc, 1) > 200 * 1024) return;
+  while (tc > 1 && tile_smem_bytes(D, tc) > 113 * 1024) tc /= 2;
   const int64_t nchunks = (ncols + tc - 1) / tc;
-  if (nchunks * P->batch < 2 * fock_num_sms() || nchunks > 65535) return;
+  if (nchunks * P->batch < 2 * fock_num_sms()) return;
   for (const PlanOp& op : P->ops)
     if (op.conj || op.owner >= 0) return;
   // predecessors
@@ -309,26 +304,16 @@ static void form_tile_groups(fock_plan* P) {
     }
   }
   if (groups.empty()) return;
-  // the adjoint writes one partial C per chunk of columns and op: keep them
-  // within the one-reduction budget (else the per-op path is cheaper)
-  double part = 0.0;
-  for (const fock_plan::Group& g : groups)
-    for (int k = g.k0; k < g.k1; ++k)
-      part += (double)nchunks * layout_entries(P->ops[order[k]].layout, D) * P->batch * sizeof(double2);
-  if (part > 1536.0 * (1 << 20)) return;
   std::vector<PlanOp> ops;
   for (int i : order) ops.push_back(P->ops[i]);
   for (size_t gi = 0; gi < groups.size(); ++gi)
-    for (int k = groups[gi].k0; k < groups[gi].k1; ++k) {
-      ops[k].group = (int)gi;
-      ops[k].tile_gx = (int)nchunks;
-    }
+    for (int k = groups[gi].k0; k < groups[gi].k1; ++k) ops[k].group = (int)gi;
   P->ops = ops;
   P->groups = groups;
   P->tile_tc = tc;
   // forward CTAs: every chunk in one wave when the resident CTAs allow it
   // (shared memory bounds the CTAs per SM; registers allow 4)
-  const int per_sm = std::max(1, std::min(4, (int)((227 * 1024) / tile_smem_bytes(D, tc, 0))));
+  const int per_sm = std::max(1, std::min(4, (int)((227 * 1024) / tile_smem_bytes(D, tc))));
   P->tile_grid = (int)std::min<int64_t>(nchunks, (int64_t)per_sm * fock_num_sms());
 }
 
@@ -586,7 +571,6 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
       op.grid_fwd = plane_grid(dtype, op.pg_fwd, 0, batch);
       op.grid_adj = plane_grid(dtype, op.pg_adj, 1, batch);
     }
-    if (op.group >= 0) op.plane_ok = 0;  // runs in its tile group
     op.plane = op.plane_ok && (force_plane || plane_preferred(op.layout, op.view));
     if (P->persist) {
       op.psched = make_adj_sched_grid(dtype, op.view, D, op.layout, P->g_bwd);
@@ -791,8 +775,7 @@ static int sweep_ctx(fock_plan* P, unsigned char* ws, cudaStream_t st, SweepCtx*
   return FOCK_OK;
 }
 
-// kernel arguments of ops [k0, k1) of tile group gi (stores and input slots
-// left unset: -1)
+// kernel arguments of ops [k0, k1) of tile group gi (stores left unset: -1)
 static void tile_arg(const fock_plan* P, int gi, int k0, int k1, TileGroupArg* a) {
   memset(a, 0, sizeof(*a));
   const fock_plan::Group& G = P->groups[gi];
@@ -806,6 +789,8 @@ static void tile_arg(const fock_plan* P, int gi, int k0, int k1, TileGroupArg* a
   a->T = D * D * D;
   a->nops = k1 - k0;
   a->TC = P->tile_tc;
+  a->lgTC = 0;
+  while ((1 << a->lgTC) < a->TC) ++a->lgTC;
   for (int i = 0; i < 3; ++i) a->S[i] = stride(G.m[i]);
   int nr = 0;
   for (int m = 0; m < N; ++m)
@@ -831,23 +816,13 @@ static void tile_arg(const fock_plan* P, int gi, int k0, int k1, TileGroupArg* a
       t.tb = std::max(x1, x2);
       t.swap = x1 > x2;
     }
-    t.nent = (int)op.nent;
-    t.G = tile_group_g(op.layout, D, a->TC);
     t.m_off = op.m_off;
     t.store_slot = -1;
-    t.in_slot = -1;
-    t.cpart_off = op.cpart_off;
   }
 }
 
 static int apply_op(const SweepCtx& c, int k, const void* in, void* out) {
   const PlanOp& op = c.P->ops[k];
-  if (op.group >= 0) {  // one op of a tile group on its own
-    TileGroupArg a;
-    tile_arg(c.P, op.group, k, k + 1, &a);
-    a.ops[0].store_slot = 0;
-    return launch_tile_forward(a, in, out, c.arena, c.P->tile_grid, c.st, c.bt);
-  }
   if (op.plane)
     return launch_plane_apply(c.P->dtype, in, out, op.pg_fwd, op.grid_fwd, c.arena + op.m_off, op_flags(op),
                               c.st, c.bt);
@@ -944,16 +919,7 @@ static int adjoint_op(BwdCtx& b, int k, const void* psi_in) {
   if (P->timing && (rc = record_event(P->ev_bwd[k + 1], st))) return rc;
   double2* cout = (double2*)(b.ws + P->o_carena) + op.c_off;
   double2* part = b.cpart + (P->reduce_at_end ? op.cpart_off : 0);
-  if (op.group >= 0) {  // one op of a tile group on its own
-    TileGroupArg a;
-    tile_arg(P, op.group, k, k + 1, &a);
-    a.ops[0].cpart_off = 0;
-    rc = launch_tile_adjoint(a, psi_in, psi_in, b.lam, b.other, b.c.arena, part, st, b.c.bt);
-    if (rc) return rc;
-    if (!P->reduce_at_end)
-      rc = launch_reduce_partials(part, op.tile_gx, op.nent, cout, st, P->batch, P->cpart_entries,
-                                  P->carena_entries, b.pdl);
-  } else if (op.plane) {
+  if (op.plane) {
     rc = launch_plane_adjoint(P->dtype, psi_in, b.lam, b.other, op.pg_adj, op.grid_adj, b.c.arena + op.m_off,
                               op_flags(op), part, st, b.c.bt);
     if (rc) return rc;
@@ -1101,22 +1067,8 @@ extern "C" int fock_plan_backward_recompute(fock_plan* P, const double* params, 
   b.pdl = !P->timing;
   b.c.bt.pdl = 0;
   if (K == 1) {
-    for (int k = n_ops - 1; k >= 0; --k) {
-      const PlanOp& op = P->ops[k];
-      if (op.group >= 0 && !P->timing && P->reduce_at_end && P->groups[op.group].k1 - 1 == k) {
-        // a whole tile group in one launch, lam kept in shared memory
-        const int k0 = P->groups[op.group].k0;
-        TileGroupArg a;
-        tile_arg(P, op.group, k0, k + 1, &a);
-        for (int j = k0; j <= k; ++j) a.ops[j - k0].in_slot = j - 1;  // -1: state_in
-        if ((rc = launch_tile_adjoint(a, state_in, states, b.lam, b.other, c.arena, b.cpart, st, b.c.bt))) return rc;
-        b.c.bt.pdl = b.pdl;
-        std::swap(b.lam, b.other);
-        k = k0;
-        continue;
-      }
+    for (int k = n_ops - 1; k >= 0; --k)
       if ((rc = adjoint_op(b, k, k == 0 ? state_in : (const char*)states + (int64_t)(k - 1) * c.sb))) return rc;
-    }
   } else {
     std::vector<void*> pool;
     for (int i = seg_slots - 1; i >= 0; --i) pool.push_back((char*)seg + (int64_t)i * c.sb);

@@ -1,5 +1,6 @@
-"""Fused tile groups (csrc/tile.cu): a complex64 pure-state plan whose ops are
-grouped on three-mode tiles against the same plan without groups
+"""Fused tile groups of the forward sweep (csrc/tile.cu): a complex64
+pure-state plan whose ops are grouped on three-mode tiles against the same
+plan without groups
 (FOCK_GB300_TILE_GROUPS=0) and against the complex128 sweep: forward states,
 stored states, gradients, batches, checkpointed sweeps and the captured
 graph.  Bars: states 1e-5 (complex64 against complex64 / complex128);
@@ -48,7 +49,7 @@ def _n_groups(circ):
 
 
 @pytest.mark.parametrize("N,D,layers,batch", [(6, 12, 2, 1), (7, 6, 2, 1), (6, 8, 2, 4), (5, 12, 1, 16),
-                                              (6, 16, 1, 1)])
+                                              (6, 14, 1, 1), (5, 16, 1, 4)])
 def test_grouped_matches_plain_and_fp64(cuda, monkeypatch, N, D, layers, batch):
     import torch
     from strawberryfields_gb300.qnn import qnn_gates, qnn_params, target_state
@@ -84,7 +85,7 @@ def test_grouped_checkpointed_and_recomputed(cuda, monkeypatch):
     from strawberryfields_gb300 import CompiledCircuit
     from strawberryfields_gb300.qnn import qnn_gates, qnn_params, target_state
 
-    N, D = 6, 10
+    N, D = 6, 12
     gates, npar = qnn_gates(N, 2)
     p = torch.tensor(qnn_params(gates, npar, seed=21), device=cuda)
     t = torch.as_tensor(target_state(N, D, 4, seed=5), device=cuda)
