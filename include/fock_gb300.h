@@ -240,7 +240,8 @@ int fock_plan_op(const fock_plan* plan, int k, int* kind, int* mode1, int* mode2
  * group's first op and its number of ops.  A complex64 pure-state plan with
  * cutoff <= 16 and enough columns groups consecutive ops whose modes lie in
  * one set of three modes; each group runs as one launch over tiles held in
- * shared memory (FOCK_GB300_TILE_GROUPS=0 at plan creation turns this off).
+ * shared memory, when FOCK_GB300_TILE_GROUPS=1 at plan creation (off by
+ * default: measured slower than per-op launches on GB300).
  * Ops are reordered only where they commute (no shared mode), so every
  * mode's ops keep their order.  No reference counterpart (the reference
  * applies every gate as its own pass over the state). */

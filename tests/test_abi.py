@@ -312,10 +312,9 @@ def test_tile_groups_keep_every_modes_order(lib, monkeypatch, N, D, layers, batc
     from strawberryfields_gb300.qnn import qnn_gates
 
     gates, npar = qnn_gates(N, layers)
-    monkeypatch.setenv("FOCK_GB300_TILE_GROUPS", "0")
-    plain = _plan_ops(lib, N, D, gates, npar, batch)
+    plain = _plan_ops(lib, N, D, gates, npar, batch)  # groups are off by default
     assert all(o[4] == -1 for o in plain)
-    monkeypatch.delenv("FOCK_GB300_TILE_GROUPS")
+    monkeypatch.setenv("FOCK_GB300_TILE_GROUPS", "1")
     grouped = _plan_ops(lib, N, D, gates, npar, batch)
     assert len(grouped) == len(plain)
     assert any(o[4] >= 0 for o in grouped)
@@ -339,11 +338,12 @@ def test_tile_groups_keep_every_modes_order(lib, monkeypatch, N, D, layers, batc
         k += count
 
 
-def test_tile_groups_only_where_they_apply(lib):
+def test_tile_groups_only_where_they_apply(lib, monkeypatch):
     """No groups for complex128, density matrices, cutoffs above 16 or too few
     columns (4 modes at cutoff 15: 15 columns)."""
     from strawberryfields_gb300.qnn import qnn_gates
 
+    monkeypatch.setenv("FOCK_GB300_TILE_GROUPS", "1")
     g6, n6 = qnn_gates(6, 1)
     assert all(o[4] == -1 for o in _plan_ops(lib, 6, 12, g6, n6, dtype=1))
     assert all(o[4] == -1 for o in _plan_ops(lib, 6, 17, g6, n6))

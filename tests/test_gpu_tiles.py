@@ -1,10 +1,9 @@
-"""Fused tile groups of the forward sweep (csrc/tile.cu): a complex64
-pure-state plan whose ops are grouped on three-mode tiles against the same
-plan without groups
-(FOCK_GB300_TILE_GROUPS=0) and against the complex128 sweep: forward states,
-stored states, gradients, batches, checkpointed sweeps and the captured
-graph.  Bars: states 1e-5 (complex64 against complex64 / complex128);
-gradients 1e-5 relative L2."""
+"""Fused tile groups of the forward sweep (csrc/tile.cu, on with
+FOCK_GB300_TILE_GROUPS=1): a complex64 pure-state plan whose ops are grouped on
+three-mode tiles against the same plan without groups (the default) and
+against the complex128 sweep -- forward states, gradients (the adjoint sweep
+reads the states the grouped forward stored), batches, checkpointed sweeps and
+the captured graph.  Bars: states 1e-5; gradients 1e-5 relative L2."""
 import numpy as np
 import pytest
 
@@ -26,11 +25,11 @@ def _pair(monkeypatch, N, D, gates, npar, **kw):
     import torch
     from strawberryfields_gb300 import CompiledCircuit
 
+    monkeypatch.setenv("FOCK_GB300_TILE_GROUPS", "1")
     grouped = CompiledCircuit(N, D, gates, npar, dtype=torch.complex64, **kw)
-    monkeypatch.setenv("FOCK_GB300_TILE_GROUPS", "0")
+    monkeypatch.delenv("FOCK_GB300_TILE_GROUPS")
     plain = CompiledCircuit(N, D, gates, npar, dtype=torch.complex64, **kw)
     c128 = CompiledCircuit(N, D, gates, npar, dtype=torch.complex128, **kw)
-    monkeypatch.delenv("FOCK_GB300_TILE_GROUPS")
     return grouped, plain, c128
 
 
@@ -78,9 +77,15 @@ def test_grouped_matches_plain_and_fp64(cuda, monkeypatch, N, D, layers, batch):
     assert float(torch.max(torch.abs(fin0 - psi_p))) < 1e-5
 
 
-def test_grouped_checkpointed_and_recomputed(cuda, monkeypatch):
-    """Checkpointed sweep (store every k-th state, recompute segments with
-    single-op tile launches) and a bounded recomputation pool."""
+@pytest.fixture
+def groups_on(monkeypatch):
+    monkeypatch.setenv("FOCK_GB300_TILE_GROUPS", "1")
+
+
+def test_grouped_checkpointed_and_recomputed(cuda, groups_on):
+    """Checkpointed sweep (the grouped forward stores every k-th state; the
+    adjoint recomputes segments with per-op launches) and a bounded
+    recomputation pool."""
     import torch
     from strawberryfields_gb300 import CompiledCircuit
     from strawberryfields_gb300.qnn import qnn_gates, qnn_params, target_state
@@ -99,8 +104,8 @@ def test_grouped_checkpointed_and_recomputed(cuda, monkeypatch):
 
 
 def test_grouped_state_in_gradient_and_graph(cuda, monkeypatch):
-    """dL/dstate_in through the grouped adjoint, and the whole step captured
-    as one CUDA graph replaying the grouped launches."""
+    """dL/dstate_in of a grouped plan, and the whole step captured as one CUDA
+    graph replaying the grouped launches."""
     import torch
     from strawberryfields_gb300.autograd import GraphedGradient
     from strawberryfields_gb300.qnn import qnn_gates, qnn_params, target_state
