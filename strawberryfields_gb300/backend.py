@@ -160,6 +160,16 @@ class FockGB300Backend:
     def prepare_fock_state(self, n, mode):
         self.circuit.prepare_mode_fock(n, self._remap_modes(mode))
 
+    def prepare_gkp(self, state, epsilon, ampl_cutoff, representation="real", shape="square", mode=None):
+        """Finite-energy GKP qubit state [theta, phi] on ``mode`` (reference
+        fockbackend/backend.py:297-329)."""
+        if representation == "complex":
+            raise NotImplementedError("The complex description of GKP is not implemented")
+        if shape != "square":
+            raise NotImplementedError("Only square GKP are implemented for now")
+        theta, phi = state[0], state[1]
+        self.circuit.prepare_mode_gkp(theta, phi, epsilon, ampl_cutoff, self._remap_modes(mode))
+
     def prepare_ket_state(self, state, modes):
         self.circuit.prepare_multimode(np.asarray(state), self._remap_modes(modes))
 

@@ -159,6 +159,9 @@ class BatchedDeviceCircuit:
             float(self._per_copy(r_d, b)), float(self._per_copy(phi_d, b)), float(self._per_copy(r_s, b)),
             float(self._per_copy(phi_s, b)), mode))
 
+    def prepare_mode_gkp(self, theta, phi, epsilon, ampl_cutoff, mode):
+        self._each(lambda dc, b: dc.prepare_mode_gkp(theta, phi, epsilon, ampl_cutoff, mode))
+
     def prepare_mode_thermal(self, nbar, mode):
         self._each(lambda dc, b: dc.prepare_mode_thermal(float(self._per_copy(nbar, b)), mode))
 

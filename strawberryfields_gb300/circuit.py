@@ -419,6 +419,36 @@ class DeviceCircuit:
         vec = self.gate_matrix(L.DISPLACEMENT, r_d, phi_d, De) @ s
         self.prepare(vec[:D].cpu().numpy(), mode)
 
+    def prepare_mode_gkp(self, theta, phi, epsilon, ampl_cutoff, mode):
+        """Finite-energy square-lattice GKP qubit
+        cos(theta/2)|0>_gkp + e^{-i phi} sin(theta/2)|1>_gkp (reference
+        circuit.py:803 and ops.py:518-599): each logical state is a sum over
+        lattice teeth t of displaced squeezed vacua D(a_t) S(r)|0>, with
+        a_t = sqrt(pi/2)(2t + mu)/cosh(eps), weight exp(-pi/2 tanh(eps)(2t + mu)^2),
+        r = -log(tanh eps)/2, and the teeth |t| <= ceil(sqrt(-log(ampl_cutoff)
+        / (4 pi tanh eps))) -- the reference's finite-energy definition.  The
+        displaced squeezed vacua are the device-built gate matrices applied
+        at an extended cutoff (exact truncated amplitudes up to the tail of
+        the squeezed vacuum past it), then normalised."""
+        D = self._trunc
+        De = 64
+        th = math.tanh(epsilon)
+        z_max = int(np.ceil(np.sqrt(-0.25 / np.pi * np.log(ampl_cutoff) / th)))
+        r = -0.5 * math.log(th)
+        sq = self.gate_matrix(L.SQUEEZE, r, 0.0, De)[:, 0]
+        kets = []
+        for mu in (0, 1):
+            v = torch.zeros(D, dtype=torch.complex128, device=self._device)
+            for t in range(-z_max, z_max + 1):
+                a = math.sqrt(0.5 * np.pi) * (2 * t + mu) / math.cosh(epsilon)
+                w = math.exp(-0.5 * np.pi * th * (mu + 2 * t) ** 2)
+                disp = self.gate_matrix(L.DISPLACEMENT, abs(a), np.pi if a < 0 else 0.0, De)
+                v = v + w * (disp @ sq)[:D]
+            kets.append(v)
+        ket = math.cos(theta / 2) * kets[0] + math.sin(theta / 2) * np.exp(-1j * phi) * kets[1]
+        ket = ket / torch.linalg.vector_norm(ket)
+        self.prepare(ket.cpu().numpy(), mode)
+
     def prepare_mode_thermal(self, nbar, mode):
         D = self._trunc
         if nbar == 0:

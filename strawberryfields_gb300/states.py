@@ -236,8 +236,8 @@ class FockStateGB300:
         from math import factorial
 
         D = self._cutoff
-        vecs = [np.array([np.exp(-0.5 * abs(a) ** 2) * a ** k / np.sqrt(factorial(k)) for k in range(D)])
-                for a in alpha_list]
+        vecs = [np.array([np.exp(-0.5 * abs(a) ** 2) * a ** k / np.sqrt(factorial(k)) for k in range(D)],
+                         dtype=np.complex128) for a in alpha_list]
         dev = self._tensor.device
         if self._pure:
             x = self._tensor.to(torch.complex128)

@@ -342,6 +342,41 @@ def test_add_and_delete_modes_match_reference_backend(cuda, pure):
     assert np.abs(red_got - red_ref).max() < TOL
 
 
+@pytest.mark.parametrize("pure", [True, False])
+@pytest.mark.parametrize("state,eps,D", [([0, 0], 0.2, 12), ([np.pi / 2, 0.4], 0.3, 20), ([1.1, 2.0], 0.25, 30)])
+def test_gkp_matches_reference_backend(cuda, pure, state, eps, D):
+    """prepare_gkp against the reference's FockBackend (fockbackend/backend.py:
+    297-329, square lattice, real representation) on the second mode of a
+    two-mode state, at 1e-8 (the device builds each tooth's displaced
+    squeezed vacuum at cutoff 64, the reference from its closed form); the
+    logical-zero state has parity +1 (reference tests/integration/
+    test_utils_integration.py:290-300) and the unsupported forms raise."""
+    from oracle import sfref
+
+    try:
+        sfref.import_strawberryfields()
+    except ImportError:
+        pytest.skip("reference sources not available")
+    from strawberryfields.backends.fockbackend import FockBackend
+    from strawberryfields_gb300 import FockGB300Backend
+
+    dms = []
+    for cls in (FockBackend, FockGB300Backend):
+        b = cls()
+        b.begin_circuit(2, cutoff_dim=D, pure=pure)
+        b.displacement(0.3, 0.1, 0)
+        b.prepare_gkp(state, eps, 1e-12, mode=1)
+        dms.append(b.state().dm())
+        if cls is FockGB300Backend:
+            if state == [0, 0]:
+                assert abs(b.state().parity_expectation([1]) - 1) < 1e-6
+            with pytest.raises(NotImplementedError):
+                b.prepare_gkp(state, eps, 1e-12, representation="complex", mode=0)
+            with pytest.raises(NotImplementedError):
+                b.prepare_gkp(state, eps, 1e-12, shape="hexagonal", mode=0)
+    assert np.abs(dms[1] - dms[0]).max() < 1e-8
+
+
 def test_program_with_new_and_del_runs_unchanged(cuda):
     """A program that creates and deletes modes (ops.New / ops.Del,
     strawberryfields/ops.py:2376,2423) gives the reference fock backend's
