@@ -170,10 +170,27 @@ class ClockSampler:
                 ["nvidia-smi", "-i", str(self.index),
                  "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
                  "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"],
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "25"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, ValueError):
             self.proc = None
+            return
+        # wait for the first sample so the sampler is live when the timed
+        # region starts; samples from before mark() are not counted
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 10.0 and self._lines() == 0 and self.proc.poll() is None:
+            time.sleep(0.02)
+
+    def _lines(self):
+        try:
+            with open(self.path) as f:
+                return sum(1 for _ in f)
+        except OSError:
+            return 0
+
+    def mark(self):
+        """Start of the timed region: only samples written after it count."""
+        self.first = self._lines()
 
     def stop(self):
         if self.proc is None:
@@ -185,7 +202,11 @@ class ClockSampler:
             self.proc.kill()
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        lines = open(self.path).readlines()
+        first = getattr(self, "first", 0)
+        if len(lines) > first:
+            lines = lines[first:]
+        for line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 7:
                 continue
@@ -369,6 +390,7 @@ def gpu_arm(args, rank, world, cpu_base):
     clocks.start()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     torch.cuda.synchronize()
+    clocks.mark()
     wall0 = time.perf_counter()
     for k in range(args.steps):
         flush.zero_()
@@ -863,7 +885,7 @@ def batched_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
