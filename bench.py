@@ -567,10 +567,11 @@ def gpu_arm(args, rank, world, cpu_base):
         torch.cuda.empty_cache()
         extra["config5_lossy_dm_4x14"] = lossy_run(dev, steps=2, warmup=1, fp64=args.lossy_fp64)
 
-    # ours per step (as the ncu launch list shows): one matrix build (the
-    # adjoint sweep reuses the forward sweep's matrices), nops applies, nops
-    # adjoints, one reduction of every op's partial sums, parameter gradients
-    launches = 2 * nops + 3
+    # ours per step (as the ncu launch list shows): one matrix build and its
+    # complex64 copy (the adjoint sweep reuses the forward sweep's matrices),
+    # nops applies, nops adjoints, one reduction of every op's partial sums,
+    # parameter gradients
+    launches = 2 * nops + 4
     cpu_fwd = cpu_base.get("forward_s_per_core") if isinstance(cpu_base, dict) else None
     out = {
         "metric": "CV-QNN grads/s (batched adjoint vs plain kernel+FD, <=1e-5 err); HBM % of peak",

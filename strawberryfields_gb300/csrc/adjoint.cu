@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)
   psi_in += blockIdx.z * bt.state_stride;
   lam_out += blockIdx.z * bt.state_stride;
   if (write_lam) lam_in += blockIdx.z * bt.state_stride;
-  mat += blockIdx.z * bt.mat_stride;
+  mat = mat_batch(mat, blockIdx.z * bt.mat_stride, mflags);
   cpart += blockIdx.z * bt.part_stride;
   const int b = layout == LAYOUT_DENSE ? 0 : block_of_y(D, y);
   const BlockGeom g = block_geom(v, D, layout, b, (mflags & MF_SWAP) ? 1 : 0);
@@ -58,10 +58,13 @@ __global__ void __launch_bounds__(TILE, AdjMinBlocks<CT, DMAX>::value)
   CT* MsH = reinterpret_cast<CT*>(smem_raw);
   CT* lam_s = MsH + ((ms_slots(sizeof(CT) == 8 ? FOCK_C64 : FOCK_C128, D) + 1) & ~(size_t)1);
   CT* psi_s = lam_s + rows * (TILE + 1);
+  // the matrix was built before the sweep: stage it while the previous op
+  // finishes
+  if (write_lam) StageDispatch<CT, kSStep, DMAX>::run(MsH, mat, g, mflags | MF_ADJOINT);
   pdl_wait();
   pdl_launch_dependents();
   AdjDispatch<CT, kSStep, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s, g, mypart,
-                                      xrank, gxb, write_lam);
+                                      xrank, gxb, write_lam, 1);
 }
 
 static int tile_of(int dtype) { return dtype == FOCK_C64 ? 256 : 128; }

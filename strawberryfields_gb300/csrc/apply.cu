@@ -58,16 +58,19 @@ __global__ void __launch_bounds__(APPLY_THREADS, ApplyMinBlocks<DMAX>::value) ap
   CT* Ms = reinterpret_cast<CT*>(smem_raw);
   in += blockIdx.z * bt.state_stride;
   out += blockIdx.z * bt.state_stride;
-  mat += blockIdx.z * bt.mat_stride;
+  mat = mat_batch(mat, blockIdx.z * bt.mat_stride, mflags);
   // grid (column tiles, blocks) or, interleaved (il), (blocks, column tiles)
   const int yb = il ? (int)blockIdx.x : (int)blockIdx.y;
   const int64_t tile = il ? (int64_t)blockIdx.y : (int64_t)blockIdx.x;
   const int b = layout == LAYOUT_DENSE ? 0 : block_of_y(D, yb);
   const BlockGeom g = block_geom(v, D, layout, b, (mflags & MF_SWAP) ? 1 : 0);
   const int64_t j0 = tile * (APPLY_THREADS * APPLY_COLS) + threadIdx.x;
+  // the matrix was built before the sweep: stage it while the previous op
+  // finishes
+  StageDispatch<CT, kSStep, DMAX>::run(Ms, mat, g, mflags);
   pdl_wait();
   pdl_launch_dependents();
-  ApplyDispatch<CT, kSStep, DMAX>::run(in, out, v, D, Ms, mat, mflags, g, j0);
+  ApplyDispatch<CT, kSStep, DMAX>::run(in, out, v, D, Ms, mat, mflags, g, j0, 1);
 }
 
 template <typename CT, int DMAX>

@@ -60,6 +60,7 @@ __device__ __forceinline__ int64_t col_base(const AxisView& v, int64_t j, int D)
 #define MF_CONJ 1     // use conj(M)            (bra side of a mixed state)
 #define MF_ADJOINT 2  // use M^dagger           (adjoint sweep)
 #define MF_SWAP 4     // view axes are (mode2, mode1) of the stored two-mode matrix
+#define MF_F32 8      // mat holds complex64 copies of the entries (float2), not double2
 
 // geometry of block b of a view: s entries, offsets base + boff + u*step
 struct BlockGeom {
@@ -129,6 +130,27 @@ __host__ __device__ __forceinline__ size_t ms_slots(int, int D) {
   return (size_t)D * ((D + kSStep - 1) / kSStep * kSStep + 2);
 }
 
+// Matrix entry idx (FP64, or the complex64 copy with MF_F32) in the state
+// precision, conjugated when cj; and the batch offset of a matrix pointer.
+template <typename CT>
+__device__ __forceinline__ CT mat_entry(const double2* mat, int64_t idx, int cj, int mflags) {
+  if (sizeof(CT) == 8 && (mflags & MF_F32)) {
+    float2 m = reinterpret_cast<const float2*>(mat)[idx];
+    if (cj) m.y = -m.y;
+    CT v;
+    v.x = m.x;
+    v.y = m.y;
+    return v;
+  }
+  double2 m = mat[idx];
+  if (cj) m.y = -m.y;
+  return to_c(m, (CT*)nullptr);
+}
+__device__ __forceinline__ const double2* mat_batch(const double2* mat, int64_t entries, int mflags) {
+  if (mflags & MF_F32) return reinterpret_cast<const double2*>(reinterpret_cast<const float2*>(mat) + entries);
+  return mat + entries;
+}
+
 // Stage the s x s block for this CTA into shared memory in the state precision,
 // as the matrix that maps the view's input positions to its output positions
 // (row w at Ms + w * ms_stride(s)).
@@ -140,10 +162,8 @@ __device__ __forceinline__ void stage_block(CT* Ms, const double2* mat, const Bl
     int a = w, c = u;
     if (mflags & MF_ADJOINT) { a = u; c = w; }  // (M^dag)[w][u] = conj(M[u][w])
     if (g.rev) { a = s - 1 - a; c = s - 1 - c; }
-    double2 m = mat[g.moff + (int64_t)a * s + c];
-    int cj = ((mflags & MF_ADJOINT) ? 1 : 0) ^ ((mflags & MF_CONJ) ? 1 : 0);
-    if (cj) m.y = -m.y;
-    Ms[w * sp + u] = to_c(m, (CT*)nullptr);
+    const int cj = ((mflags & MF_ADJOINT) ? 1 : 0) ^ ((mflags & MF_CONJ) ? 1 : 0);
+    Ms[w * sp + u] = mat_entry<CT>(mat, g.moff + (int64_t)a * s + c, cj, mflags);
   }
 }
 
@@ -160,9 +180,7 @@ __device__ __forceinline__ void stage_block_pad(CT* Ms, const double2* mat, cons
       int a = w, c = u;
       if (mflags & MF_ADJOINT) { a = u; c = w; }
       if (g.rev) { a = s - 1 - a; c = s - 1 - c; }
-      double2 m = mat[g.moff + (int64_t)a * s + c];
-      if (cj) m.y = -m.y;
-      v = to_c(m, (CT*)nullptr);
+      v = mat_entry<CT>(mat, g.moff + (int64_t)a * s + c, cj, mflags);
     }
     Ms[w * sp + u] = v;
   }

@@ -26,10 +26,12 @@ __device__ __forceinline__ CT ld_state(const CT* p) {
 
 // The column's loads are issued before the block is staged in shared memory,
 // so the two global round trips overlap.
+// staged: the block is in shared memory already (the kernel staged it before
+// waiting for its stream predecessor)
 template <typename CT, int S, bool COH>
 __device__ __forceinline__ void apply_cols(const CT* __restrict__ in, CT* __restrict__ out,
                                            const AxisView& v, int D, CT* Ms, const double2* mat, int mflags,
-                                           const BlockGeom& g, int64_t j0) {
+                                           const BlockGeom& g, int64_t j0, int staged) {
   const bool valid = j0 < v.ncols;
   const int s = g.s;  // <= S
   const int64_t b0 = valid ? col_base(v, j0, D) + g.boff : 0;
@@ -57,7 +59,7 @@ __device__ __forceinline__ void apply_cols(const CT* __restrict__ in, CT* __rest
       for (int u = 0; u < S; ++u) x0[u] = u < s ? ld_state<COH>(in + b0 + u * g.step) : czero<CT>();
     }
   }
-  stage_block_pad<CT, S>(Ms, mat, g, mflags);
+  if (!staged) stage_block_pad<CT, S>(Ms, mat, g, mflags);
   __syncthreads();
   if (!valid) return;
   constexpr int SP = sizeof(CT) == 8 ? (S + 1) & ~1 : S;
@@ -88,8 +90,8 @@ __device__ __forceinline__ void apply_cols(const CT* __restrict__ in, CT* __rest
 template <typename CT, bool COH>
 __device__ void apply_cols_generic(const CT* __restrict__ in, CT* __restrict__ out, const AxisView& v,
                                    int D, CT* Ms, const double2* mat, int mflags, const BlockGeom& g,
-                                   int64_t j0) {
-  stage_block(Ms, mat, g, mflags);
+                                   int64_t j0, int staged) {
+  if (!staged) stage_block(Ms, mat, g, mflags);
   __syncthreads();
   for (int k = 0; k < APPLY_COLS; ++k) {
     const int64_t j = j0 + k * APPLY_THREADS;
@@ -108,16 +110,34 @@ __device__ void apply_cols_generic(const CT* __restrict__ in, CT* __restrict__ o
 template <typename CT, int S, int DMAX, bool COH = false>
 struct ApplyDispatch {
   __device__ __forceinline__ static void run(const CT* in, CT* out, const AxisView& v, int D, CT* Ms,
-                                             const double2* mat, int mflags, const BlockGeom& g, int64_t j0) {
-    if (g.s <= S) apply_cols<CT, S, COH>(in, out, v, D, Ms, mat, mflags, g, j0);
-    else ApplyDispatch<CT, S + kSStep, DMAX, COH>::run(in, out, v, D, Ms, mat, mflags, g, j0);
+                                             const double2* mat, int mflags, const BlockGeom& g, int64_t j0,
+                                             int staged = 0) {
+    if (g.s <= S) apply_cols<CT, S, COH>(in, out, v, D, Ms, mat, mflags, g, j0, staged);
+    else ApplyDispatch<CT, S + kSStep, DMAX, COH>::run(in, out, v, D, Ms, mat, mflags, g, j0, staged);
   }
 };
 template <typename CT, int DMAX, bool COH>
 struct ApplyDispatch<CT, DMAX + kSStep, DMAX, COH> {
   __device__ __forceinline__ static void run(const CT* in, CT* out, const AxisView& v, int D, CT* Ms,
-                                             const double2* mat, int mflags, const BlockGeom& g, int64_t j0) {
-    apply_cols_generic<CT, COH>(in, out, v, D, Ms, mat, mflags, g, j0);
+                                             const double2* mat, int mflags, const BlockGeom& g, int64_t j0,
+                                             int staged = 0) {
+    apply_cols_generic<CT, COH>(in, out, v, D, Ms, mat, mflags, g, j0, staged);
+  }
+};
+
+// The block staged as the body of size S >= s that the dispatch above picks
+// (the layout apply_cols / adjoint_body read), or as the generic loop's block.
+template <typename CT, int S, int DMAX>
+struct StageDispatch {
+  __device__ __forceinline__ static void run(CT* Ms, const double2* mat, const BlockGeom& g, int mflags) {
+    if (g.s <= S) stage_block_pad<CT, S>(Ms, mat, g, mflags);
+    else StageDispatch<CT, S + kSStep, DMAX>::run(Ms, mat, g, mflags);
+  }
+};
+template <typename CT, int DMAX>
+struct StageDispatch<CT, DMAX + kSStep, DMAX> {
+  __device__ __forceinline__ static void run(CT* Ms, const double2* mat, const BlockGeom& g, int mflags) {
+    stage_block(Ms, mat, g, mflags);
   }
 };
 
@@ -146,7 +166,7 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
                                              CT* __restrict__ lam_in, const AxisView& v, int D, CT* MsH,
                                              const double2* __restrict__ mat, int mflags, CT* lam_s, CT* psi_s,
                                              const BlockGeom& g, double2* __restrict__ mypart, int xrank, int gxb,
-                                             int write_lam) {
+                                             int write_lam, int staged) {
   constexpr int RR = RRof<S>::value;
   constexpr int NG = TILE / 16;
   constexpr int LD = TILE + 1;  // padded row stride (elements)
@@ -178,7 +198,7 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
   };
   // the first tile's copies are in flight while the block is staged
   if (xrank < ntiles) issue(xrank);
-  if (write_lam) stage_block_pad<CT, S>(MsH, mat, g, mflags | MF_ADJOINT);
+  if (write_lam && !staged) stage_block_pad<CT, S>(MsH, mat, g, mflags | MF_ADJOINT);
   // padding rows S..4*RR-1 stay zero
   for (int e = tid; e < (4 * RR - S) * LD; e += TILE) {
     lam_s[S * LD + e] = czero<CT>();
@@ -251,8 +271,8 @@ template <typename CT, int TILE>
 __device__ void adjoint_generic(const CT* __restrict__ psi_in, const CT* __restrict__ lam_out,
                                 CT* __restrict__ lam_in, const AxisView& v, int D, CT* MsH,
                                 const double2* __restrict__ mat, int mflags, const BlockGeom& g,
-                                double2* __restrict__ mypart, int xrank, int gxb, int write_lam) {
-  if (write_lam) stage_block(MsH, mat, g, mflags | MF_ADJOINT);
+                                double2* __restrict__ mypart, int xrank, int gxb, int write_lam, int staged) {
+  if (write_lam && !staged) stage_block(MsH, mat, g, mflags | MF_ADJOINT);
   __syncthreads();
   // large blocks (beyond the unrolled buckets): thread per C entry over this
   // CTA's share of the columns, then lam_in per column
@@ -288,13 +308,13 @@ struct AdjDispatch {
   __device__ __forceinline__ static void run(const CT* psi_in, const CT* lam_out, CT* lam_in, const AxisView& v,
                                              int D, CT* MsH, const double2* mat, int mflags, CT* lam_s, CT* psi_s,
                                              const BlockGeom& g, double2* mypart, int xrank, int gxb,
-                                             int write_lam) {
+                                             int write_lam, int staged = 0) {
     if (g.s <= S)
       adjoint_body<CT, S, TILE>(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s, g, mypart, xrank,
-                                gxb, write_lam);
+                                gxb, write_lam, staged);
     else
       AdjDispatch<CT, S + kSStep, DMAX, TILE>::run(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, lam_s, psi_s,
-                                                   g, mypart, xrank, gxb, write_lam);
+                                                   g, mypart, xrank, gxb, write_lam, staged);
   }
 };
 template <typename CT, int DMAX, int TILE>
@@ -302,8 +322,9 @@ struct AdjDispatch<CT, DMAX + kSStep, DMAX, TILE> {
   __device__ __forceinline__ static void run(const CT* psi_in, const CT* lam_out, CT* lam_in, const AxisView& v,
                                              int D, CT* MsH, const double2* mat, int mflags, CT*, CT*,
                                              const BlockGeom& g, double2* mypart, int xrank, int gxb,
-                                             int write_lam) {
-    adjoint_generic<CT, TILE>(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, g, mypart, xrank, gxb, write_lam);
+                                             int write_lam, int staged = 0) {
+    adjoint_generic<CT, TILE>(psi_in, lam_out, lam_in, v, D, MsH, mat, mflags, g, mypart, xrank, gxb, write_lam,
+                              staged);
   }
 };
 

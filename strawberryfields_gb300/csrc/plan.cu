@@ -98,6 +98,10 @@ struct fock_plan {
   int tile_grid = 0;   // CTAs of a forward group launch
   size_t o_sweep = 0, o_sync = 0, o_ppart = 0;
   int64_t ppart_entries = 0;
+  // complex64 plans: the sweep kernels stage complex64 copies of the
+  // matrices (o_arena32, converted after every build), not the FP64 arena
+  int mat32 = 0;
+  size_t o_arena32 = 0;
   // optional per-op timing
   int timing = 0;
   std::vector<cudaEvent_t> ev_fwd, ev_bwd;
@@ -529,6 +533,9 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   // CV-QNN the per-op launches with programmatic dependent launch measured
   // 2.3 ms per forward against 3.6 ms for the persistent sweep, whose grid
   // barrier alone costs about 3 us per op)
+  // FOCK_GB300_MAT32=0 keeps the FP64 matrices in the sweep kernels' staging
+  const char* m32 = getenv("FOCK_GB300_MAT32");
+  P->mat32 = dtype == FOCK_C64 && !(m32 && atoi(m32) == 0);
   const char* sw = getenv("FOCK_GB300_SWEEP_MAX_BYTES");
   const int64_t sweep_max = sw ? (int64_t)atoll(sw) : 0;
   const int64_t sbytes = elems * (dtype == FOCK_C64 ? 8 : 16);
@@ -607,6 +614,7 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
   P->tables_bytes = o;
   P->o_arena = o; o = align256(o + sizeof(double2) * arena * batch);
   P->o_carena = o; o = align256(o + sizeof(double2) * std::max<int64_t>(carena, 1) * batch);
+  if (P->mat32) { P->o_arena32 = o; o = align256(o + sizeof(float2) * std::max<int64_t>(arena, 1) * batch); }
   P->o_cpart = o;
   P->ppart_entries = ppart;
   layout_partials(P);
@@ -732,6 +740,13 @@ extern "C" int fock_plan_op(const fock_plan* P, int k, int* kind, int* mode1, in
 // ---------------------------------------------------------------------------
 // execution
 // ---------------------------------------------------------------------------
+// complex64 copies of the built matrices (every arena entry of every circuit)
+__global__ void arena32_kernel(const double2* __restrict__ a, float2* __restrict__ o, int64_t n) {
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += step)
+    o[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
 static int upload_and_build(fock_plan* P, const double* params, unsigned char* ws, int with_deriv,
                             cudaStream_t st) {
   FOCK_CUDA_TRY(cudaMemcpyAsync(ws, P->host, P->tables_bytes, cudaMemcpyHostToDevice, st));
@@ -741,8 +756,15 @@ static int upload_and_build(fock_plan* P, const double* params, unsigned char* w
     // table; building dM as well costs one extra matrix write per op and keeps
     // one table
   }
-  return launch_build_jobs((const BuildJob*)(ws + P->o_jobs), P->n_jobs, (const PhaseTerm*)(ws + P->o_terms),
-                           params, (double2*)(ws + P->o_arena), st, P->batch, P->n_params, P->arena_entries);
+  int rc = launch_build_jobs((const BuildJob*)(ws + P->o_jobs), P->n_jobs, (const PhaseTerm*)(ws + P->o_terms),
+                             params, (double2*)(ws + P->o_arena), st, P->batch, P->n_params, P->arena_entries);
+  if (rc || !P->mat32) return rc;
+  const int64_t n = P->arena_entries * P->batch;
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, 4096);
+  arena32_kernel<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>((const double2*)(ws + P->o_arena),
+                                                                        (float2*)(ws + P->o_arena32), n);
+  FOCK_LAUNCH_CHECK("arena32_kernel");
+  return FOCK_OK;
 }
 
 // grid-barrier words of a persistent sweep, cleared before every launch
@@ -760,6 +782,7 @@ static int sweep_sync(fock_plan* P, unsigned char* ws, cudaStream_t st, SweepSyn
 struct SweepCtx {
   fock_plan* P;
   const double2* arena;
+  const float2* arena32;  // complex64 copies (mat32 plans), or null
   BatchArg bt;
   int64_t sb;  // bytes of one slot (whole batch)
   cudaStream_t st;
@@ -770,6 +793,7 @@ static int sweep_ctx(fock_plan* P, unsigned char* ws, cudaStream_t st, SweepCtx*
   c->P = P;
   c->sb = P->state_elems * esz * P->batch;
   c->arena = (const double2*)(ws + P->o_arena);
+  c->arena32 = P->mat32 ? (const float2*)(ws + P->o_arena32) : nullptr;
   c->bt.nb = P->batch;
   c->bt.state_stride = P->state_elems;
   c->bt.mat_stride = P->arena_entries;
@@ -824,12 +848,19 @@ static void tile_arg(const fock_plan* P, int gi, int k0, int k1, TileGroupArg* a
   }
 }
 
+// the matrix of op k for the sweep kernels, and its staging flags
+static const double2* sweep_mat(const SweepCtx& c, const PlanOp& op) {
+  if (c.arena32) return reinterpret_cast<const double2*>(c.arena32 + op.m_off);
+  return c.arena + op.m_off;
+}
+static int sweep_flags(const SweepCtx& c, const PlanOp& op) { return op_flags(op) | (c.arena32 ? MF_F32 : 0); }
+
 static int apply_op(const SweepCtx& c, int k, const void* in, void* out) {
   const PlanOp& op = c.P->ops[k];
   if (op.plane)
-    return launch_plane_apply(c.P->dtype, in, out, op.pg_fwd, op.grid_fwd, c.arena + op.m_off, op_flags(op),
+    return launch_plane_apply(c.P->dtype, in, out, op.pg_fwd, op.grid_fwd, sweep_mat(c, op), sweep_flags(c, op),
                               c.st, c.bt);
-  return launch_apply(c.P->dtype, in, out, op.view, c.P->D, op.layout, c.arena + op.m_off, op_flags(op),
+  return launch_apply(c.P->dtype, in, out, op.view, c.P->D, op.layout, sweep_mat(c, op), sweep_flags(c, op),
                       c.st, c.bt);
 }
 
@@ -923,15 +954,15 @@ static int adjoint_op(BwdCtx& b, int k, const void* psi_in) {
   double2* cout = (double2*)(b.ws + P->o_carena) + op.c_off;
   double2* part = b.cpart + (P->reduce_at_end ? op.cpart_off : 0);
   if (op.plane) {
-    rc = launch_plane_adjoint(P->dtype, psi_in, b.lam, b.other, op.pg_adj, op.grid_adj, b.c.arena + op.m_off,
-                              op_flags(op), part, st, b.c.bt);
+    rc = launch_plane_adjoint(P->dtype, psi_in, b.lam, b.other, op.pg_adj, op.grid_adj, sweep_mat(b.c, op),
+                              sweep_flags(b.c, op), part, st, b.c.bt);
     if (rc) return rc;
     if (!P->reduce_at_end)
       rc = launch_reduce_partials(part, op.grid_adj, op.nent, cout, st, P->batch, P->cpart_entries,
                                   P->carena_entries, b.pdl);
   } else {
-    rc = launch_adjoint_partials(P->dtype, psi_in, b.lam, b.other, op.view, P->D, op.layout, b.c.arena + op.m_off,
-                                 op_flags(op), part, op.sched, st, b.c.bt);
+    rc = launch_adjoint_partials(P->dtype, psi_in, b.lam, b.other, op.view, P->D, op.layout, sweep_mat(b.c, op),
+                                 sweep_flags(b.c, op), part, op.sched, st, b.c.bt);
     if (rc) return rc;
     if (!P->reduce_at_end)
       rc = launch_reduce_sched(part, op.sched, P->D, op.layout, cout, st, P->batch, P->cpart_entries,

@@ -168,9 +168,7 @@ __device__ __forceinline__ void pl_stage(CT* Ms, const double2* __restrict__ mat
     int a = w, c = u;
     if (mflags & MF_ADJOINT) { a = u; c = w; }
     if (g.rev[y]) { a = s - 1 - a; c = s - 1 - c; }
-    double2 m = mat[g.moff[y] + a * s + c];
-    if (cj) m.y = -m.y;
-    Ms[idx] = to_c(m, (CT*)nullptr);
+    Ms[idx] = mat_entry<CT>(mat, g.moff[y] + a * s + c, cj, mflags);
   }
 }
 
@@ -246,17 +244,19 @@ __global__ void __launch_bounds__(PL_THREADS, 2)
   const int64_t tsz = (int64_t)g.TC * g.EP;
   in += blockIdx.z * bt.state_stride;
   out += blockIdx.z * bt.state_stride;
-  mat += blockIdx.z * bt.mat_stride;
+  mat = mat_batch(mat, blockIdx.z * bt.mat_stride, mflags);
   const int64_t G = gridDim.x;
   int64_t t = blockIdx.x;
   pl_offsets(goff, g);
   pl_bases(cb0, g, t);
   pl_bases(cb0 + g.TC, g, t + G);
+  // the matrices were built before the sweep: staged while the previous op
+  // finishes
+  pl_stage(Ms, mat, g, mflags);
   __syncthreads();
   pdl_wait();
   pdl_launch_dependents();
   if (t < g.ntiles) pl_issue(in, T0, g, goff, cb0, pl_cols(g.TC, g.ncols - t * g.TC));
-  pl_stage(Ms, mat, g, mflags);  // overlaps the first tile's copies
   int buf = 0;
   // buffer buf holds tile t (bases cb0 + buf*TC); buf^1 receives tile t + G
   for (; t < g.ntiles; t += G) {
@@ -296,13 +296,16 @@ __global__ void __launch_bounds__(PL_THREADS, 2)
   psi_in += blockIdx.z * bt.state_stride;
   lam_out += blockIdx.z * bt.state_stride;
   if (lam_in) lam_in += blockIdx.z * bt.state_stride;
-  mat += blockIdx.z * bt.mat_stride;
+  mat = mat_batch(mat, blockIdx.z * bt.mat_stride, mflags);
   cpart += blockIdx.z * bt.part_stride + (int64_t)blockIdx.x * g.nent;
   const int64_t GX = gridDim.x;
   int64_t t = blockIdx.x;
   pl_offsets(goff, g);
   pl_bases(cb0, g, t);
   pl_bases(cb0 + g.TC, g, t + GX);
+  // the matrices were built before the sweep: staged while the previous op
+  // finishes
+  if (lam_in) pl_stage(MsH, mat, g, mflags | MF_ADJOINT);
   __syncthreads();
   pdl_wait();
   pdl_launch_dependents();
@@ -311,7 +314,6 @@ __global__ void __launch_bounds__(PL_THREADS, 2)
     pl_issue(lam_out, L, g, goff, cb0, tcv);
     pl_issue(psi_in, P, g, goff, cb0, tcv);
   }
-  if (lam_in) pl_stage(MsH, mat, g, mflags | MF_ADJOINT);
 
   // C slots of this thread: slot i = tid + k * PL_THREADS is entry i % nent
   // summed over the columns col = i / nent (mod G)
