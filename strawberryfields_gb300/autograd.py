@@ -256,9 +256,10 @@ class CompiledCircuit:
         """Pick each op's kernel family, block-adjoint CTAs per SM and plane
         tile columns by timing a forward + adjoint sweep at ``params`` under
         every candidate (per-op CUDA events, best of ``repeats``), keeping per
-        op the candidate with the smallest forward + adjoint time.  The tuned
-        plan is kept only when its whole step (PDL launches, final reduction)
-        is faster than the configuration it started from.  Returns
+        op the candidate with the smallest forward + adjoint time.  The whole
+        step (PDL launches, final reduction) then decides between these picks,
+        the picks with the starting CTA densities, each with one plane tile
+        width for every plane op, and the configuration it started from.  Returns
         ``(configs, ms_before, ms_after)`` with configs[k] =
         (family, ctas, tile columns)."""
         if self.n_ops == 0:
@@ -307,8 +308,13 @@ class CompiledCircuit:
         picks = [(fam, c if fam == 0 else start[k][1], tc if fam == 1 else start[k][3])
                  for k, (fam, c, tc) in enumerate(best)]
         no_ctas = [(fam, start[k][1], tc) for k, (fam, c, tc) in enumerate(picks)]
+        # and of one tile width for every plane op: per-op events favour wider
+        # tiles on the adjoint, while the step on an L2-resident state can
+        # prefer the narrower tiles' extra resident CTAs for every plane op
+        uniform = [[(fam, c, tw if fam == 1 else tc) for fam, c, tc in base]
+                   for tw in tiles for base in (picks, no_ctas) if any(f == 1 for f, _, _ in base)]
         results = [(ms_before, start_cfg)]
-        for cfg in (picks, no_ctas):
+        for cfg in [picks, no_ctas] + uniform:
             if cfg != start_cfg and all(cfg != r[1] for r in results):
                 apply(cfg)
                 results.append((self._timed_sweeps(p, lam, repeats, False), cfg))

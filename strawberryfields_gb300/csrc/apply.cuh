@@ -345,6 +345,8 @@ int launch_reduce_sched(const double2* cpart, const AdjSched& sc, int D, int lay
 #define PL_WARPS 8
 #define PL_MAX_BLK 48
 #define PL_MAX_ITEMS 128
+#define PL_RT 3            // C pass: each thread sums a PL_RT x PL_RT sub-block of one block's C
+#define PL_MAX_CITEMS 384  // C sub-blocks of the largest plane (366 at cutoff 16)
 #define PL_MAX_D1 24  // one-mode ops up to this cutoff
 #define PL_MAX_D2 16  // two-mode ops up to this cutoff (D*D <= PL_THREADS rows)
 struct PlaneGeom {
@@ -353,7 +355,8 @@ struct PlaneGeom {
   int two, c_inner;       // two-mode plane; copy with lanes over columns
   int flat;               // plane of column j starts at j*E (gate on the innermost axes)
   unsigned emagic;        // ceil(2^26 / E): idx / E as a multiply-shift
-  int nblk, G, nslot;     // blocks; column groups and (entry, group) slots of the C pass
+  int nblk, G, nslot;     // blocks; column groups and (sub-block, group) slots of the C pass
+  int ncitems;            // C sub-blocks (PL_RT x PL_RT)
   int nent, ms_total;     // C entries (= staged matrix entries)
   int sm_goff, sm_cb, sm_tile, smem;  // shared-memory layout (bytes)
   short base[PL_MAX_BLK], step[PL_MAX_BLK], s[PL_MAX_BLK];  // block y: elements base + u*step
@@ -363,6 +366,7 @@ struct PlaneGeom {
   unsigned char rev[PL_MAX_BLK];
   short warp_start[PL_WARPS + 1];
   unsigned short items[PL_MAX_ITEMS];  // (block << 4) | column group, per warp
+  unsigned short citems[PL_MAX_CITEMS];  // (block << 10) | (row0 << 5) | col0 of each C sub-block
 };
 // 0 when the op does not fit the plane kernels (then the block kernels run)
 // tile_columns: columns per tile of a two-mode plane op (0: 32)

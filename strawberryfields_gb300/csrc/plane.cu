@@ -56,14 +56,20 @@ __device__ __forceinline__ void pl_commit() { asm volatile("cp.async.commit_grou
 template <int N>
 __device__ __forceinline__ void pl_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// C entries of the largest plane with blocks up to SMAX: the sum or
-// difference blocks of a two-mode op (sizes 1..D..1, D(2D^2+1)/3 entries) up
-// to PL_MAX_D2, one dense block of a one-mode op beyond; and the C slots per
-// thread of the adjoint that covers them
-__host__ __device__ constexpr int pl_nent_max(int smax) {
-  return smax <= PL_MAX_D2 ? smax * (2 * smax * smax + 1) / 3 : smax * smax;
+// C sub-blocks (PL_RT x PL_RT) of the largest plane with blocks up to smax,
+// and the sub-blocks per thread of the C pass that covers them
+__host__ __device__ constexpr int pl_ceil_rt(int s) { return (s + PL_RT - 1) / PL_RT; }
+__host__ __device__ constexpr int pl_citems_max(int smax) {
+  int n = 0;
+  if (smax <= PL_MAX_D2) {
+    for (int s = 1; s <= smax; ++s) n += 2 * pl_ceil_rt(s) * pl_ceil_rt(s);
+    n -= pl_ceil_rt(smax) * pl_ceil_rt(smax);
+  } else {
+    n = pl_ceil_rt(smax) * pl_ceil_rt(smax);
+  }
+  return n;
 }
-__host__ __device__ constexpr int pl_kmax(int smax) { return (pl_nent_max(smax) + PL_THREADS - 1) / PL_THREADS; }
+__host__ __device__ constexpr int pl_ki(int smax) { return (pl_citems_max(smax) + PL_THREADS - 1) / PL_THREADS; }
 
 // columns of a tile that starts at column j0 (the last tile may be partial)
 __device__ __forceinline__ int pl_cols(int64_t tc, int64_t rest) { return (int)(rest < tc ? rest : tc); }
@@ -315,28 +321,31 @@ __global__ void __launch_bounds__(PL_THREADS, 2)
     pl_issue(psi_in, P, g, goff, cb0, tcv);
   }
 
-  // C slots of this thread: slot i = tid + k * PL_THREADS is entry i % nent
-  // summed over the columns col = i / nent (mod G)
-  constexpr int KMAX = pl_kmax(SMAX);
+  // C pass: thread slot i = tid + k * PL_THREADS sums the PL_RT x PL_RT
+  // sub-block citems[i % ncitems] of one block's C over the columns
+  // col = i / ncitems (mod G) -- each shared load feeds PL_RT complex FMAs
+  constexpr int KI = pl_ki(SMAX);
   const int G = g.G;
-  short loff[KMAX], poff[KMAX], grp[KMAX];
-  int cout[KMAX];
-  CT acc[KMAX];
+  int lb[KI], pb[KI], st[KI], nr[KI], nc[KI], grp[KI];
+  CT acc[KI][PL_RT][PL_RT];
 #pragma unroll
-  for (int k = 0; k < KMAX; ++k) {
-    acc[k] = czero<CT>();
+  for (int k = 0; k < KI; ++k) {
     const int i = tid + k * PL_THREADS;
     grp[k] = -1;
+    lb[k] = pb[k] = st[k] = nr[k] = nc[k] = 0;
+#pragma unroll
+    for (int r = 0; r < PL_RT; ++r)
+#pragma unroll
+      for (int c = 0; c < PL_RT; ++c) acc[k][r][c] = czero<CT>();
     if (i < g.nslot) {
-      const int e = i % g.nent;
-      int y = 0;
-      while (y + 1 < g.nblk && e >= g.ms_off[y + 1]) ++y;
-      const int s = g.s[y], r = e - g.ms_off[y], u = r / s, w = r - u * s;
-      loff[k] = (short)(g.base[y] + u * g.step[y]);
-      poff[k] = (short)(g.base[y] + w * g.step[y]);
-      const int a = g.rev[y] ? s - 1 - u : u, b = g.rev[y] ? s - 1 - w : w;
-      cout[k] = g.cout_off[y] + a * s + b;
-      grp[k] = (short)(i / g.nent);
+      const int it = g.citems[i % g.ncitems];
+      const int y = it >> 10, r0 = (it >> 5) & 31, c0 = it & 31, s = g.s[y];
+      st[k] = g.step[y];
+      lb[k] = g.base[y] + r0 * st[k];
+      pb[k] = g.base[y] + c0 * st[k];
+      nr[k] = s - r0 < PL_RT ? s - r0 : PL_RT;
+      nc[k] = s - c0 < PL_RT ? s - c0 : PL_RT;
+      grp[k] = i / g.ncitems;
     }
   }
 
@@ -350,11 +359,22 @@ __global__ void __launch_bounds__(PL_THREADS, 2)
     pl_wait<0>();
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < KMAX; ++k) {
+    for (int k = 0; k < KI; ++k) {
       if (grp[k] < 0) break;
-      const CT* lr = L + loff[k];
-      const CT* pr = P + poff[k];
-      for (int col = grp[k]; col < tcv; col += G) cfma_conj(acc[k], lr[col * g.EP], pr[col * g.EP]);
+      for (int col = grp[k]; col < tcv; col += G) {
+        const CT* lr = L + col * g.EP + lb[k];
+        const CT* pr = P + col * g.EP + pb[k];
+        CT lv[PL_RT], pv[PL_RT];
+#pragma unroll
+        for (int r = 0; r < PL_RT; ++r) {
+          lv[r] = r < nr[k] ? lr[r * st[k]] : czero<CT>();
+          pv[r] = r < nc[k] ? pr[r * st[k]] : czero<CT>();
+        }
+#pragma unroll
+        for (int r = 0; r < PL_RT; ++r)
+#pragma unroll
+          for (int c = 0; c < PL_RT; ++c) cfma_conj(acc[k][r][c], lv[r], pv[c]);
+      }
     }
     __syncthreads();
     const int tcn = tn < g.ntiles ? pl_cols(g.TC, g.ncols - tn * g.TC) : 0;
@@ -372,27 +392,42 @@ __global__ void __launch_bounds__(PL_THREADS, 2)
   pl_wait<0>();
   __syncthreads();
   // partial C of this CTA (stored orientation)
+  auto put = [&](int it, int r, int c, double2 v) {
+    const int y = it >> 10, u = ((it >> 5) & 31) + r, w = (it & 31) + c, s = g.s[y];
+    if (u >= s || w >= s) return;
+    const int a = g.rev[y] ? s - 1 - u : u, b = g.rev[y] ? s - 1 - w : w;
+    cpart[g.cout_off[y] + a * s + b] = v;
+  };
   if (G == 1) {
 #pragma unroll
-    for (int k = 0; k < KMAX; ++k)
-      if (grp[k] >= 0) cpart[cout[k]] = to_d(acc[k]);
-  } else {
-    // sum the G column groups of each entry through shared memory (fixed order)
-    CT* red = L;
+    for (int k = 0; k < KI; ++k) {
+      if (grp[k] < 0) break;
+      const int it = g.citems[(tid + k * PL_THREADS) % g.ncitems];
 #pragma unroll
-    for (int k = 0; k < KMAX; ++k)
-      if (grp[k] >= 0) red[tid + k * PL_THREADS] = acc[k];
+      for (int r = 0; r < PL_RT; ++r)
+#pragma unroll
+        for (int c = 0; c < PL_RT; ++c) put(it, r, c, to_d(acc[k][r][c]));
+    }
+  } else {
+    // G > 1 only when KI = 1: sum the G column groups of each sub-block entry
+    // through shared memory (fixed order)
+    CT* red = L;
+    if (grp[0] >= 0) {
+#pragma unroll
+      for (int r = 0; r < PL_RT; ++r)
+#pragma unroll
+        for (int c = 0; c < PL_RT; ++c) red[tid * PL_RT * PL_RT + r * PL_RT + c] = acc[0][r][c];
+    }
     __syncthreads();
-    // G > 1 only when nent <= PL_THREADS / 2: entry tid's group-0 slot is
-    // this thread's slot 0
-    if (tid < g.nent) {
+    for (int e = tid; e < g.ncitems * PL_RT * PL_RT; e += PL_THREADS) {
+      const int item = e / (PL_RT * PL_RT), rc = e - item * PL_RT * PL_RT;
       double2 sum = make_double2(0.0, 0.0);
       for (int q = 0; q < G; ++q) {
-        const double2 v = to_d(red[q * g.nent + tid]);
+        const double2 v = to_d(red[(q * g.ncitems + item) * PL_RT * PL_RT + rc]);
         sum.x += v.x;
         sum.y += v.y;
       }
-      cpart[cout[0]] = sum;
+      put(g.citems[item], rc / PL_RT, rc % PL_RT, sum);
     }
   }
 }
@@ -451,10 +486,18 @@ int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, i
   g.ms_off[g.nblk] = ms;
   g.ms_total = ms;
   g.nent = ms;
-  // C pass: one slot per entry, times G column groups when entries are few
-  g.G = std::max(1, PL_THREADS / ms);
-  g.nslot = ms * g.G;
-  if (g.nslot > PL_THREADS * pl_kmax(D)) return 0;
+  // C pass: PL_RT x PL_RT sub-blocks of every block's C, times G column
+  // groups when there are few sub-blocks
+  g.ncitems = 0;
+  for (int y = 0; y < g.nblk; ++y)
+    for (int r0 = 0; r0 < g.s[y]; r0 += PL_RT)
+      for (int c0 = 0; c0 < g.s[y]; c0 += PL_RT) {
+        if (g.ncitems >= PL_MAX_CITEMS) return 0;
+        g.citems[g.ncitems++] = (unsigned short)((y << 10) | (r0 << 5) | c0);
+      }
+  g.G = std::max(1, PL_THREADS / g.ncitems);
+  g.nslot = g.ncitems * g.G;
+  if (g.nslot > PL_THREADS * pl_ki(dmax_bucket(D))) return 0;
   // columns per tile: one warp of columns per block for two modes; enough
   // column groups to give every warp a dense block otherwise
   // two-mode planes: tile_columns (8..32; default 32) -- fewer columns give
@@ -493,7 +536,7 @@ int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, i
   g.sm_cb = (int)align16((size_t)g.sm_goff + (size_t)g.E * 8);
   g.sm_tile = (int)align16((size_t)g.sm_cb + (size_t)2 * g.TC * 8);
   size_t tiles = (size_t)2 * g.TC * g.EP * esz;
-  if (adjoint) tiles = std::max(tiles, (size_t)g.nslot * esz);  // column-group reduction
+  if (adjoint) tiles = std::max(tiles, (size_t)g.nslot * PL_RT * PL_RT * esz);  // column-group reduction
   g.smem = (int)(g.sm_tile + tiles);
   if (g.smem > 200 * 1024) return 0;
   *out = g;
