@@ -252,64 +252,87 @@ int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* 
 }
 
 
-// every op's partial sums at once (one warp per C entry, lanes over the
-// op's CTAs, fixed order)
-__global__ void reduce_ops_kernel(const RedOp* __restrict__ ops, int n_ops, int64_t total, int D,
-                                  const double2* __restrict__ cpart, double2* __restrict__ carena,
-                                  int64_t part_stride, int64_t out_stride) {
+// every op's partial sums at once.  One CTA per chunk of ec consecutive C
+// entries of one op (ec = 32, 16 or 8 by the op's partial-row count gx): the
+// CTA's K = 256 / ec row segments each sum rows x = k, k + K, ... of the
+// chunk's entries (a row's entries are contiguous, so the loads are whole
+// 128-byte lines or more), then the K segment sums of each entry are added
+// in order.  The order is fixed by the plan, so the result does not depend on
+// timing.
+__global__ void __launch_bounds__(RED_THREADS)
+    reduce_ops_kernel(const RedOp* __restrict__ ops, int n_ops, int D, const double2* __restrict__ cpart,
+                      double2* __restrict__ carena, int64_t part_stride, int64_t out_stride) {
   pdl_wait();
   pdl_launch_dependents();
-  const int lane = threadIdx.x & 31;
-  const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  __shared__ double2 red[RED_THREADS];
   cpart += blockIdx.y * part_stride;
   carena += blockIdx.y * out_stride;
-  if (e >= total) return;
+  const int chunk = (int)blockIdx.x;
   int lo = 0, hi = n_ops - 1;
-  while (lo < hi) {  // last op with c_off <= e
+  while (lo < hi) {  // last op whose first chunk is <= this one
     const int mid = (lo + hi + 1) >> 1;
-    if (ops[mid].c_off <= e) lo = mid;
+    if (ops[mid].chunk0 <= chunk) lo = mid;
     else hi = mid - 1;
   }
   const RedOp R = ops[lo];
-  const int64_t le = e - R.c_off;
-  const double2* src;
-  int64_t stride;
-  if (R.plane) {
-    src = cpart + R.cpart_off + le;
-    stride = R.nent;
-  } else if (R.layout == LAYOUT_DENSE) {
-    src = cpart + R.cpart_off + le;
-    stride = (int64_t)D * D;
-  } else {
-    int bs = 0, s = 1;
-    int64_t off = 0;
-    for (bs = 0; bs < 2 * D - 1; ++bs) {
-      s = blk_size(D, bs);
-      if (le < off + (int64_t)s * s) break;
-      off += (int64_t)s * s;
-    }
-    src = cpart + R.cpart_off + (int64_t)R.gx * off + (le - off);
-    stride = (int64_t)s * s;
-  }
+  const int ec = R.ec, K = RED_THREADS / ec;
+  const int i = threadIdx.x % ec, k = threadIdx.x / ec;
+  const int64_t le = (int64_t)(chunk - R.chunk0) * ec + i;
   double2 a = make_double2(0.0, 0.0);
-  for (int x = lane; x < R.gx; x += 32) {
-    const double2 p = src[(int64_t)x * stride];
-    a.x += p.x;
-    a.y += p.y;
+  if (le < R.nent) {
+    // partial rows of entry le: [gx][nent] (plane), [gx][D*D] (dense), or
+    // the entry's block [gx][s*s] at gx * (entries of the earlier blocks)
+    const double2* src;
+    int64_t stride;
+    if (R.plane) {
+      src = cpart + R.cpart_off + le;
+      stride = R.nent;
+    } else if (R.layout == LAYOUT_DENSE) {
+      src = cpart + R.cpart_off + le;
+      stride = (int64_t)D * D;
+    } else {
+      int bs = 0, s = 1;
+      int64_t off = 0;
+      for (bs = 0; bs < 2 * D - 1; ++bs) {
+        s = blk_size(D, bs);
+        if (le < off + (int64_t)s * s) break;
+        off += (int64_t)s * s;
+      }
+      src = cpart + R.cpart_off + (int64_t)R.gx * off + (le - off);
+      stride = (int64_t)s * s;
+    }
+    int x = k;
+    for (; x + 3 * K < R.gx; x += 4 * K) {
+      const double2 p0 = src[(int64_t)x * stride];
+      const double2 p1 = src[(int64_t)(x + K) * stride];
+      const double2 p2 = src[(int64_t)(x + 2 * K) * stride];
+      const double2 p3 = src[(int64_t)(x + 3 * K) * stride];
+      a.x += p0.x; a.y += p0.y;
+      a.x += p1.x; a.y += p1.y;
+      a.x += p2.x; a.y += p2.y;
+      a.x += p3.x; a.y += p3.y;
+    }
+    for (; x < R.gx; x += K) {
+      const double2 p = src[(int64_t)x * stride];
+      a.x += p.x; a.y += p.y;
+    }
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
-    a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
+  red[threadIdx.x] = a;
+  __syncthreads();
+  if (k == 0 && le < R.nent) {
+    for (int q = 1; q < K; ++q) {
+      a.x += red[q * ec + i].x;
+      a.y += red[q * ec + i].y;
+    }
+    carena[R.c_off + le] = a;
   }
-  if (lane == 0) carena[e] = a;
 }
 
-int launch_reduce_ops(const RedOp* ops, int n_ops, int64_t total, int D, const double2* cpart, double2* carena,
+int launch_reduce_ops(const RedOp* ops, int n_ops, int64_t chunks, int D, const double2* cpart, double2* carena,
                       cudaStream_t st, int nb, int64_t part_stride, int64_t out_stride) {
-  if (total <= 0) return FOCK_OK;
-  const int64_t blocks = (total * 32 + 255) / 256;
-  FOCK_CUDA_TRY(launch_kernel(reduce_ops_kernel, dim3((unsigned)blocks, nb), dim3(256), 0, st, 0, ops, n_ops, total, D,
-                               cpart, carena, part_stride, out_stride));
+  if (chunks <= 0) return FOCK_OK;
+  if (chunks > 0x7fffffffLL) return fock_set_error(FOCK_ERR_INVALID, "too many reduction chunks");
+  FOCK_CUDA_TRY(launch_kernel(reduce_ops_kernel, dim3((unsigned)chunks, nb), dim3(RED_THREADS), 0, st, 0,
+                               ops, n_ops, D, cpart, carena, part_stride, out_stride));
   return FOCK_OK;
 }

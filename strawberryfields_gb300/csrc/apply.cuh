@@ -330,8 +330,14 @@ int launch_reduce_partials(const double2* cpart, int gx, int64_t nent, double2* 
 struct RedOp {
   int64_t c_off, cpart_off;
   int nent, gx, plane, layout;
+  int chunk0;  // first reduction CTA of this op
+  int ec;      // C entries per reduction CTA: 32, 16 or 8 (more partial rows, fewer entries)
 };
-int launch_reduce_ops(const RedOp* ops, int n_ops, int64_t total, int D, const double2* cpart, double2* carena,
+#define RED_THREADS 256
+// entries per reduction CTA for an op with gx partial rows: the CTA's
+// RED_THREADS / ec row segments keep each thread's serial sum short
+__host__ __device__ __forceinline__ int red_entries_per_cta(int gx) { return gx <= 128 ? 32 : gx <= 512 ? 16 : 8; }
+int launch_reduce_ops(const RedOp* ops, int n_ops, int64_t chunks, int D, const double2* cpart, double2* carena,
                       cudaStream_t st, int nb, int64_t part_stride, int64_t out_stride);
 // sum the partials of a schedule into `cout` (stored orientation, layout entries)
 int launch_reduce_sched(const double2* cpart, const AdjSched& sc, int D, int layout, double2* cout, cudaStream_t st,

@@ -217,8 +217,17 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
       for (int u = 0; u < S; ++u) lam[u] = lam_s[u * LD + tid];
       ColRegs<CT, S> lc;
       lc.set(lam);
+      // two rows per pass: four independent FMA chains instead of two
+      int w = 0;
 #pragma unroll 1
-      for (int w = 0; w < s; ++w) {
+      for (; w + 1 < s; w += 2) {
+        CT a0 = czero<CT>(), a1 = czero<CT>();
+        row_mac<S>(a0, MsH + w * SP, lc);
+        row_mac<S>(a1, MsH + (w + 1) * SP, lc);
+        lam_in[base + w * g.step] = a0;
+        lam_in[base + (w + 1) * g.step] = a1;
+      }
+      if (w < s) {
         CT a = czero<CT>();
         row_mac<S>(a, MsH + w * SP, lc);
         lam_in[base + w * g.step] = a;

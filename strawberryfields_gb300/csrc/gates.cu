@@ -102,6 +102,31 @@ __device__ __forceinline__ int dev_layout_entries(int layout, int D) {
   return layout == LAYOUT_DENSE ? D * D : blk_total(D);
 }
 
+// Per-CTA tables of a build.  The recurrences scale by sqrt(k) and 1/sqrt(k)
+// of small integers, and the fused phases are exp(i angle) of index
+// functions; FP64 square roots, divisions and sincos are long instruction
+// sequences on GB300's FP64 pipe (1/64 of the FP32 rate), so each value is
+// computed once per CTA instead of once per matrix entry.  The table entries
+// are the same correctly rounded sqrt(k) and 1.0 / sqrt(k) the per-entry
+// expressions gave.
+#define BUILD_SQ_N (2 * FOCK_MAX_CUTOFF + 8)
+#define BUILD_PH_D 24  // phase tables for cutoffs up to 24 (two D x D tables)
+struct BuildTab {
+  double sq[BUILD_SQ_N];
+  double isq[BUILD_SQ_N];
+  double2 ph[2][BUILD_PH_D * BUILD_PH_D];  // exp(i angle) of the input / output side
+};
+
+__device__ void build_tab_sqrt(BuildTab& T, int D) {
+  const int n = min(2 * D + 8, BUILD_SQ_N);
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const double r = sqrt((double)k);
+    T.sq[k] = r;
+    T.isq[k] = k > 0 ? 1.0 / r : 0.0;
+  }
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // builders (whole CTA); U -> M, dU/dp0 -> dM (may be null)
 // ---------------------------------------------------------------------------
@@ -109,14 +134,14 @@ __device__ __forceinline__ int dev_layout_entries(int layout, int D) {
 // Displacement: D[0,n] = e^{-r^2/2} (-conj(alpha))^n / sqrt(n!),
 // sqrt(m+1) D[m+1,n] = sqrt(n) D[m,n-1] + alpha D[m,n];
 // dD/dr[m,n] = e^{i phi} sqrt(m) D[m-1,n] - e^{-i phi} sqrt(n) D[m,n-1] - r D[m,n].
-__device__ void build_displacement(double r, double phi, int D, double2* M, double2* dM) {
+__device__ void build_displacement(double r, double phi, int D, double2* M, double2* dM, const BuildTab& T) {
   const double2 alpha = dscale(dexpi(phi), r);
   if (threadIdx.x == 0) {
     double2 v = make_double2(exp(-0.5 * r * r), 0.0);
     const double2 mac = make_double2(-alpha.x, alpha.y);  // -conj(alpha)
     M[0] = v;
     for (int n = 1; n < D; ++n) {
-      v = dscale(dmul(v, mac), 1.0 / sqrt((double)n));
+      v = dscale(dmul(v, mac), T.isq[n]);
       M[n] = v;
     }
   }
@@ -124,8 +149,8 @@ __device__ void build_displacement(double r, double phi, int D, double2* M, doub
   for (int m = 0; m < D - 1; ++m) {
     for (int n = threadIdx.x; n < D; n += blockDim.x) {
       double2 acc = dmul(alpha, M[m * D + n]);
-      if (n > 0) acc = cadd(acc, dscale(M[m * D + n - 1], sqrt((double)n)));
-      M[(m + 1) * D + n] = dscale(acc, 1.0 / sqrt((double)(m + 1)));
+      if (n > 0) acc = cadd(acc, dscale(M[m * D + n - 1], T.sq[n]));
+      M[(m + 1) * D + n] = dscale(acc, T.isq[m + 1]);
     }
     __syncthreads();
   }
@@ -134,8 +159,8 @@ __device__ void build_displacement(double r, double phi, int D, double2* M, doub
     for (int idx = threadIdx.x; idx < D * D; idx += blockDim.x) {
       int m = idx / D, n = idx - m * D;
       double2 acc = dscale(M[idx], -r);
-      if (m > 0) acc = cadd(acc, dmul(e, dscale(M[idx - D], sqrt((double)m))));
-      if (n > 0) acc = csub(acc, dmul(ec, dscale(M[idx - 1], sqrt((double)n))));
+      if (m > 0) acc = cadd(acc, dmul(e, dscale(M[idx - D], T.sq[m])));
+      if (n > 0) acc = csub(acc, dmul(ec, dscale(M[idx - 1], T.sq[n])));
       dM[idx] = acc;
     }
   }
@@ -147,7 +172,8 @@ __device__ void build_displacement(double r, double phi, int D, double2* M, doub
 // S[m,n+1] = (sqrt(m) S[m-1,n] + e^{-i phi} sinh r sqrt(n) S[m,n-1]) / (cosh r sqrt(n+1)).
 // Built on rows 0..D+1 (scratch X, row-major (D+2) x D) so that
 // dS/dr = G S, G = (e^{-i phi} a^2 - e^{i phi} a^dag^2)/2, is exact.
-__device__ void build_squeezing(double r, double phi, int D, double2* M, double2* dM, double2* X) {
+__device__ void build_squeezing(double r, double phi, int D, double2* M, double2* dM, double2* X,
+                                const BuildTab& T) {
   const int R = D + 2;
   const double c = cosh(r), s = sinh(r), t = tanh(r);
   const double2 e = dexpi(phi), ec = make_double2(e.x, -e.y);
@@ -166,9 +192,9 @@ __device__ void build_squeezing(double r, double phi, int D, double2* M, double2
   for (int n = 0; n < D - 1; ++n) {
     for (int m = threadIdx.x; m < R; m += blockDim.x) {
       double2 acc = make_double2(0.0, 0.0);
-      if (m > 0) acc = dscale(X[(m - 1) * D + n], sqrt((double)m));
-      if (n > 0) acc = cadd(acc, dmul(ec, dscale(X[m * D + n - 1], s * sqrt((double)n))));
-      X[m * D + n + 1] = dscale(acc, 1.0 / (c * sqrt((double)(n + 1))));
+      if (m > 0) acc = dscale(X[(m - 1) * D + n], T.sq[m]);
+      if (n > 0) acc = cadd(acc, dmul(ec, dscale(X[m * D + n - 1], s * T.sq[n])));
+      X[m * D + n + 1] = dscale(acc, 1.0 / (c * T.sq[n + 1]));
     }
     __syncthreads();
   }
@@ -200,7 +226,7 @@ __device__ __forceinline__ double2 blk_get(const double2* X, int De, int ks, int
   return X[blk_offset(De, N) + u * s + v];
 }
 
-__device__ void build_beamsplitter_ext(double theta, double phi, int De, double2* X) {
+__device__ void build_beamsplitter_ext(double theta, double phi, int De, double2* X, const BuildTab& T) {
   const double t = cos(theta);
   const double2 rho = dscale(dexpi(phi), sin(theta));
   const double2 rhoc = make_double2(rho.x, -rho.y);
@@ -213,13 +239,13 @@ __device__ void build_beamsplitter_ext(double theta, double phi, int De, double2
       int i = lo + u, k = lo + v;
       double2 acc;
       if (i >= 1) {
-        acc = dscale(blk_get(X, De, 1, N - 1, i - 1, k - 1), t * sqrt((double)k));
-        acc = csub(acc, dmul(rhoc, dscale(blk_get(X, De, 1, N - 1, i - 1, k), sqrt((double)(N - k)))));
-        acc = dscale(acc, 1.0 / sqrt((double)i));
+        acc = dscale(blk_get(X, De, 1, N - 1, i - 1, k - 1), t * T.sq[k]);
+        acc = csub(acc, dmul(rhoc, dscale(blk_get(X, De, 1, N - 1, i - 1, k), T.sq[N - k])));
+        acc = dscale(acc, T.isq[i]);
       } else {
-        acc = dscale(blk_get(X, De, 1, N - 1, 0, k), t * sqrt((double)(N - k)));
-        acc = cadd(acc, dmul(rho, dscale(blk_get(X, De, 1, N - 1, 0, k - 1), sqrt((double)k))));
-        acc = dscale(acc, 1.0 / sqrt((double)N));
+        acc = dscale(blk_get(X, De, 1, N - 1, 0, k), t * T.sq[N - k]);
+        acc = cadd(acc, dmul(rho, dscale(blk_get(X, De, 1, N - 1, 0, k - 1), T.sq[k])));
+        acc = dscale(acc, T.isq[N]);
       }
       X[off + e] = acc;
     }
@@ -235,7 +261,7 @@ __device__ void build_beamsplitter_ext(double theta, double phi, int De, double2
 // T[m,n+1,p,q] = (sqrt(m) T[m-1,n,p,q] - e^{-i phi} s sqrt(q) T[m,n,p,q-1]) / (c sqrt(n+1)),
 // processed in layers of the input's first coordinate.
 // dT/dr = G T with G = e^{i phi} a1^dag a2^dag - e^{-i phi} a1 a2.
-__device__ void build_s2_ext(double r, double phi, int De, double2* X) {
+__device__ void build_s2_ext(double r, double phi, int De, double2* X, const BuildTab& T) {
   const double c = cosh(r), s = sinh(r), th = tanh(r);
   const double2 e = dexpi(phi), ec = make_double2(e.x, -e.y);
   const double2 lam = dscale(e, th);
@@ -269,9 +295,9 @@ __device__ void build_s2_ext(double r, double phi, int De, double2* X) {
         if (m >= 1 && b >= 1) t1 = blk_get(X, De, 0, b - 1, m - 1, n1 - 1);
         // T[m, n, p, q-1]: same block, input position v-1
         double2 t2 = X[blk_offset(De, b) + u * sb + (v - 1)];
-        double2 acc = dscale(t1, sqrt((double)m));
-        acc = csub(acc, dmul(ec, dscale(t2, s * sqrt((double)q))));
-        val = dscale(acc, 1.0 / (c * sqrt((double)n1)));
+        double2 acc = dscale(t1, T.sq[m]);
+        acc = csub(acc, dmul(ec, dscale(t2, s * T.sq[q])));
+        val = dscale(acc, 1.0 / (c * T.sq[n1]));
       }
       X[blk_offset(De, b) + u * sb + v] = val;
     }
@@ -282,7 +308,7 @@ __device__ void build_s2_ext(double r, double phi, int De, double2* X) {
 // copy the cutoff-D blocks out of cutoff-(D+1) storage and form G*U
 // gen_kind 0: beamsplitter generator, 1: two-mode-squeeze generator
 __device__ void blocks_truncate_and_derive(const double2* X, int D, int ks, double phi,
-                                           int gen_kind, double2* M, double2* dM) {
+                                           int gen_kind, double2* M, double2* dM, const BuildTab& T) {
   const int De = D + 1;
   const double2 e = dexpi(phi), ec = make_double2(e.x, -e.y);
   const int tot = blk_total(D);
@@ -305,12 +331,12 @@ __device__ void blocks_truncate_and_derive(const double2* X, int D, int ks, doub
       double2 acc;
       if (gen_kind == 0) {
         // e^{i phi} sqrt(m+1) sqrt(p) B[m+1, n, p-1, q] - e^{-i phi} sqrt(m) sqrt(p+1) B[m-1, n, p+1, q]
-        acc = dmul(e, dscale(blk_get(X, De, 1, be, oa + 1, ia), sqrt((oa + 1.0) * ob)));
-        acc = csub(acc, dmul(ec, dscale(blk_get(X, De, 1, be, oa - 1, ia), sqrt(oa * (ob + 1.0)))));
+        acc = dmul(e, dscale(blk_get(X, De, 1, be, oa + 1, ia), T.sq[oa + 1] * T.sq[ob]));
+        acc = csub(acc, dmul(ec, dscale(blk_get(X, De, 1, be, oa - 1, ia), T.sq[oa] * T.sq[ob + 1])));
       } else {
         // e^{i phi} sqrt(m) sqrt(p) T[m-1,n,p-1,q] - e^{-i phi} sqrt(m+1) sqrt(p+1) T[m+1,n,p+1,q]
-        acc = dmul(e, dscale(blk_get(X, De, 0, be, oa - 1, ia), sqrt((double)oa * ob)));
-        acc = csub(acc, dmul(ec, dscale(blk_get(X, De, 0, be, oa + 1, ia), sqrt((oa + 1.0) * (ob + 1.0)))));
+        acc = dmul(e, dscale(blk_get(X, De, 0, be, oa - 1, ia), T.sq[oa] * T.sq[ob]));
+        acc = csub(acc, dmul(ec, dscale(blk_get(X, De, 0, be, oa + 1, ia), T.sq[oa + 1] * T.sq[ob + 1])));
       }
       dM[idx] = acc;
     }
@@ -322,8 +348,11 @@ __device__ void blocks_truncate_and_derive(const double2* X, int D, int ks, doub
 // (strawberryfields/ops.py:1951).  The external phase is carried as a fused
 // input phase term by the caller; here M = B R_in B and dM/dphi_in =
 // B (i n1 R_in) B on complete photon-number blocks (size N+1), then truncated.
-__device__ void build_mzgate(double phi_in, int D, double2* M, double2* dM, double2* X) {
+__device__ void build_mzgate(double phi_in, int D, double2* M, double2* dM, double2* X, BuildTab& T) {
   // X: [full B blocks][B R_in][B i n1 R_in]
+  // exp(i phi_in j), j < 2D - 1, in the CTA's phase table (2D - 1 <= BUILD_PH_D^2)
+  double2* ph_in = T.ph[0];
+  for (int j = threadIdx.x; j < 2 * D - 1; j += blockDim.x) ph_in[j] = dexpi(phi_in * j);
   int64_t tot = 0;
   for (int N = 0; N <= 2 * D - 2; ++N) tot += (int64_t)(N + 1) * (N + 1);
   double2* Bf = X;
@@ -349,13 +378,13 @@ __device__ void build_mzgate(double phi_in, int D, double2* M, double2* dM, doub
         return Bf[offp + ii * sp + kk];
       };
       if (i >= 1) {
-        acc = dscale(prev(i - 1, k - 1), t * sqrt((double)k));
-        acc = csub(acc, dmul(rhoc, dscale(prev(i - 1, k), sqrt((double)(N - k)))));
-        acc = dscale(acc, 1.0 / sqrt((double)i));
+        acc = dscale(prev(i - 1, k - 1), t * T.sq[k]);
+        acc = csub(acc, dmul(rhoc, dscale(prev(i - 1, k), T.sq[N - k])));
+        acc = dscale(acc, T.isq[i]);
       } else {
-        acc = dscale(prev(0, k), t * sqrt((double)(N - k)));
-        acc = cadd(acc, dmul(rho, dscale(prev(0, k - 1), sqrt((double)k))));
-        acc = dscale(acc, 1.0 / sqrt((double)N));
+        acc = dscale(prev(0, k), t * T.sq[N - k]);
+        acc = cadd(acc, dmul(rho, dscale(prev(0, k - 1), T.sq[k])));
+        acc = dscale(acc, T.isq[N]);
       }
       Bf[off + e] = acc;
     }
@@ -369,8 +398,7 @@ __device__ void build_mzgate(double phi_in, int D, double2* M, double2* dM, doub
       int i = e / s, k = e - i * s;
       double2 a1 = make_double2(0.0, 0.0), a2 = make_double2(0.0, 0.0);
       for (int j = 0; j < s; ++j) {
-        double2 ph = dexpi(phi_in * j);
-        double2 x = dmul(dmul(Bf[off + i * s + j], ph), Bf[off + j * s + k]);
+        double2 x = dmul(dmul(Bf[off + i * s + j], ph_in[j]), Bf[off + j * s + k]);
         a1 = cadd(a1, x);
         a2 = cadd(a2, dscale(make_double2(-x.y, x.x), (double)j));
       }
@@ -466,28 +494,65 @@ __device__ void run_build_job(const BuildJob& J, const PhaseTerm* terms, const d
   double2* dM = J.dm_off >= 0 ? arena + J.dm_off : nullptr;
   double2* X = J.scratch_off >= 0 ? arena + J.scratch_off : nullptr;
   const int D = J.D;
+  __shared__ BuildTab T;
+  build_tab_sqrt(T, D);
   switch (J.gate) {
-    case FOCK_DISPLACEMENT: build_displacement(p0, p1, D, M, dM); break;
-    case FOCK_SQUEEZE: build_squeezing(p0, p1, D, M, dM, X); break;
+    case FOCK_DISPLACEMENT: build_displacement(p0, p1, D, M, dM, T); break;
+    case FOCK_SQUEEZE: build_squeezing(p0, p1, D, M, dM, X, T); break;
     case FOCK_BEAMSPLITTER:
-      build_beamsplitter_ext(p0, p1, D + 1, X);
+      build_beamsplitter_ext(p0, p1, D + 1, X, T);
       __syncthreads();
-      blocks_truncate_and_derive(X, D, 1, p1, 0, M, dM);
+      blocks_truncate_and_derive(X, D, 1, p1, 0, M, dM, T);
       break;
     case FOCK_TWO_MODE_SQUEEZE:
-      build_s2_ext(p0, p1, D + 1, X);
+      build_s2_ext(p0, p1, D + 1, X, T);
       __syncthreads();
-      blocks_truncate_and_derive(X, D, 0, p1, 1, M, dM);
+      blocks_truncate_and_derive(X, D, 0, p1, 1, M, dM, T);
       break;
-    case FOCK_MZGATE: build_mzgate(p0, D, M, dM, X); break;
+    case FOCK_MZGATE: build_mzgate(p0, D, M, dM, X, T); break;
     case FOCK_LOSS: build_loss(p0, D, M, dM); break;
     case FOCK_ROTATION:
     case FOCK_KERR:
     case FOCK_CROSS_KERR: build_diag_gate(J.gate, p0, J.layout, D, M); break;
     default: build_identity(J.layout, D, M); break;
   }
-  // fused phases: M[e] *= exp(i (sum_pre p f(in) + sum_post p f(out)))
-  if (J.nterm > 0) {
+  // fused phases: M[e] *= exp(i sum_pre p f(in)) exp(i sum_post p f(out)),
+  // from one table per side over the (a, b) coordinates (b = 0 for a dense
+  // layout) -- one sincos per coordinate pair instead of one per entry
+  if (J.nterm > 0 && D <= BUILD_PH_D) {
+    int has_in = 0, has_out = 0;
+    for (int k = 0; k < J.nterm; ++k) {
+      if (terms[J.term0 + k].side) has_out = 1;
+      else has_in = 1;
+    }
+    const int nbv = J.layout == LAYOUT_DENSE ? 1 : D;
+    for (int i = threadIdx.x; i < 2 * D * nbv; i += blockDim.x) {
+      const int side = i / (D * nbv), r = i - side * D * nbv;
+      const int a = r / nbv, b = r - a * nbv;
+      if (side ? !has_out : !has_in) continue;
+      double ang = 0.0;
+      for (int k = 0; k < J.nterm; ++k) {
+        const PhaseTerm& P = terms[J.term0 + k];
+        if (P.side != side) continue;
+        double pv = P.pidx >= 0 ? params[P.pidx] : P.value;
+        if (P.neg) pv = -pv;
+        ang += pv * phase_fn(P.fn, a, b);
+      }
+      T.ph[side][a * D + b] = dexpi(ang);
+    }
+    __syncthreads();
+    const int tot = dev_layout_entries(J.layout, D);
+    for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
+      int oa, ob, ia, ib, u, v, b;
+      entry_coords(J.layout, D, idx, oa, ob, ia, ib, u, v, b);
+      double2 ph;
+      if (has_out && has_in) ph = dmul(T.ph[1][oa * D + ob], T.ph[0][ia * D + ib]);
+      else if (has_out) ph = T.ph[1][oa * D + ob];
+      else ph = T.ph[0][ia * D + ib];
+      M[idx] = dmul(M[idx], ph);
+      if (dM) dM[idx] = dmul(dM[idx], ph);
+    }
+  } else if (J.nterm > 0) {
     const int tot = dev_layout_entries(J.layout, D);
     for (int idx = threadIdx.x; idx < tot; idx += blockDim.x) {
       int oa, ob, ia, ib, u, v, b;

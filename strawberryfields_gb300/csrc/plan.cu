@@ -81,6 +81,7 @@ struct fock_plan {
   // partial sums: one region per op, reduced by one launch after the sweep
   // (when they fit the budget), or one shared region reduced after every op
   int reduce_at_end = 0;
+  int red_chunks = 0;  // CTAs of the end-of-sweep reduction
   size_t o_red = 0;
   int64_t state_elems = 0;
   int64_t flops_fwd = 0;
@@ -194,6 +195,7 @@ static void absorb_pending(PlanOp& op, int mode, std::vector<std::vector<Pending
 // table of the one-launch reduction (in the pinned table image)
 static void write_red_table(fock_plan* P) {
   RedOp* red = (RedOp*)(P->host + P->o_red);
+  int chunks = 0;
   for (size_t k = 0; k < P->ops.size(); ++k) {
     const PlanOp& op = P->ops[k];
     red[k].c_off = op.c_off;
@@ -202,7 +204,11 @@ static void write_red_table(fock_plan* P) {
     red[k].gx = op.plane ? op.grid_adj : op.sched.gx[0];
     red[k].plane = op.plane;
     red[k].layout = op.layout;
+    red[k].chunk0 = chunks;
+    red[k].ec = red_entries_per_cta(red[k].gx);
+    chunks += (int)((op.nent + red[k].ec - 1) / red[k].ec);
   }
+  P->red_chunks = chunks;
 }
 
 // Partial-sum regions and the workspace past the C arena: they depend on
@@ -665,6 +671,19 @@ extern "C" int fock_plan_create_batch(int num_modes, int cutoff, int pure, int d
       ++c;
     }
   }
+  // longest builds first (one CTA per job): the CTA scheduler gives the
+  // first CTAs an SM each, so the jobs that share an SM are the short ones
+  auto build_cost = [](const BuildJob& J) {
+    switch (J.gate) {
+      case FOCK_MZGATE: return 4;
+      case FOCK_BEAMSPLITTER:
+      case FOCK_TWO_MODE_SQUEEZE: return 3;
+      case FOCK_LOSS: return 2;
+      default: return J.layout == LAYOUT_DENSE ? 0 : 1;
+    }
+  };
+  std::stable_sort(jobs, jobs + nj,
+                   [&](const BuildJob& a, const BuildJob& b) { return build_cost(a) > build_cost(b); });
   write_red_table(P);
   if (P->persist) {
     SweepOp* sw_ops = (SweepOp*)(P->host + P->o_sweep);
@@ -1119,7 +1138,7 @@ extern "C" int fock_plan_backward_recompute(fock_plan* P, const double* params, 
     P->bwd_recorded = 1;
   }
   if (P->reduce_at_end && n_ops > 0) {
-    rc = launch_reduce_ops((const RedOp*)(ws + P->o_red), n_ops, P->carena_entries, P->D, b.cpart,
+    rc = launch_reduce_ops((const RedOp*)(ws + P->o_red), n_ops, P->red_chunks, P->D, b.cpart,
                            (double2*)(ws + P->o_carena), st, P->batch, P->cpart_entries, P->carena_entries);
     if (rc) return rc;
   }
