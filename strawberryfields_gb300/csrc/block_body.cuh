@@ -160,6 +160,7 @@ __device__ __forceinline__ void cp_async_elem(double2* dst, const double2* src, 
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_group1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
 template <typename CT, int S, int TILE>
 __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, const CT* __restrict__ lam_out,
@@ -187,11 +188,18 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
     const bool valid = j < v.ncols;
     const int64_t base = valid ? col_base(v, j, D) + g.boff : 0;
     tile_base = base;
+    // two groups: lam_out (L2-resident, needed first for lam_in), then psi_in
 #pragma unroll
     for (int u = 0; u < S; ++u) {
       const bool vu = valid && u < s;  // rows s..S-1 zero-filled
       const int64_t off = vu ? base + u * g.step : 0;
       cp_async_elem(&lam_s[u * LD + tid], lam_out + off, vu);
+    }
+    cp_async_commit();
+#pragma unroll
+    for (int u = 0; u < S; ++u) {
+      const bool vu = valid && u < s;
+      const int64_t off = vu ? base + u * g.step : 0;
       cp_async_elem(&psi_s[u * LD + tid], psi_in + off, vu);
     }
     cp_async_commit();
@@ -206,7 +214,7 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
   }
   __syncthreads();
   for (int64_t t = xrank; t < ntiles; t += gxb) {
-    cp_async_wait_all();  // this thread's column has landed
+    cp_async_wait_group1();  // this thread's lam_out column has landed
     const int64_t j = t * TILE + tid;
     if (write_lam && j < v.ncols) {
       // each thread reads back only its own column: no barrier needed here
@@ -233,6 +241,7 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
         lam_in[base + w * g.step] = a;
       }
     }
+    cp_async_wait_all();  // and its psi_in column
     __syncthreads();  // every thread's column of tile t has landed
 #pragma unroll 2
     for (int step = 0; step < TILE / NG; ++step) {
