@@ -53,6 +53,18 @@ __device__ __forceinline__ void pl_cp(double2* dst, const double2* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src));
 }
 __device__ __forceinline__ void pl_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+
+// Blocks of size s run the unrolled body of size pl_pad(s) (s rounded up to a
+// multiple of PL_S_STEP), and are staged at that size with zero padding: half
+// the bodies of one body per size.  The warps of a tile apply blocks of
+// different sizes at once, and with one body per size the kernels stalled on
+// instruction fetch more than on anything else (GB300, cutoff 12: 1.8 and 3.3
+// fetch stalls per issued instruction in the adjoint and apply).  Steps of 2
+// measured faster than steps of 4 (fewer padded FMAs) on the QNN step.
+#ifndef PL_S_STEP
+#define PL_S_STEP 2
+#endif
+__host__ __device__ __forceinline__ int pl_pad(int s) { return (s + PL_S_STEP - 1) / PL_S_STEP * PL_S_STEP; }
 template <int N>
 __device__ __forceinline__ void pl_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
@@ -168,9 +180,13 @@ __device__ __forceinline__ void pl_stage(CT* Ms, const double2* __restrict__ mat
   for (int idx = threadIdx.x; idx < g.ms_total; idx += PL_THREADS) {
     int y = 0;
     while (y + 1 < g.nblk && idx >= g.ms_off[y + 1]) ++y;
-    const int s = g.s[y];
+    const int s = g.s[y], sp = pl_pad(s);
     const int e = idx - g.ms_off[y];
-    const int w = e / s, u = e - w * s;
+    const int w = e / sp, u = e - w * sp;
+    if (w >= s || u >= s) {
+      Ms[idx] = czero<CT>();
+      continue;
+    }
     int a = w, c = u;
     if (mflags & MF_ADJOINT) { a = u; c = w; }
     if (g.rev[y]) { a = s - 1 - a; c = s - 1 - c; }
@@ -182,10 +198,10 @@ __device__ __forceinline__ void pl_stage(CT* Ms, const double2* __restrict__ mat
 // with paired FMAs (the column as (Re, Re) / (Im, Im) pairs, entries read as
 // pairs)
 template <typename CT, int S>
-__device__ __forceinline__ void pl_block(CT* row, int base, int step, const CT* Ms) {
+__device__ __forceinline__ void pl_block(CT* row, int base, int step, const CT* Ms, int s) {
   CT x[S];
 #pragma unroll
-  for (int u = 0; u < S; ++u) x[u] = row[base + u * step];
+  for (int u = 0; u < S; ++u) x[u] = u < s ? row[base + u * step] : czero<CT>();
   if constexpr (sizeof(CT) == 8) {
     f32x2 re[S], im[S];
 #pragma unroll
@@ -195,6 +211,7 @@ __device__ __forceinline__ void pl_block(CT* row, int base, int step, const CT* 
     }
 #pragma unroll
     for (int w = 0; w < S; ++w) {
+      if (w >= s) break;
       const f32x2* m = reinterpret_cast<const f32x2*>(Ms + w * S);
       f32x2 P = 0ull, Q = 0ull;
 #pragma unroll
@@ -208,6 +225,7 @@ __device__ __forceinline__ void pl_block(CT* row, int base, int step, const CT* 
   } else {
 #pragma unroll
     for (int w = 0; w < S; ++w) {
+      if (w >= s) break;
       CT a = czero<CT>();
 #pragma unroll
       for (int u = 0; u < S; ++u) cfma(a, Ms[w * S + u], x[u]);
@@ -218,12 +236,12 @@ __device__ __forceinline__ void pl_block(CT* row, int base, int step, const CT* 
 template <typename CT, int S, int SMAX>
 struct PlBlock {
   __device__ __forceinline__ static void run(int s, CT* row, int base, int step, const CT* Ms) {
-    if (s == S) pl_block<CT, S>(row, base, step, Ms);
-    else PlBlock<CT, S + 1, SMAX>::run(s, row, base, step, Ms);
+    if (s <= S) pl_block<CT, S>(row, base, step, Ms, s);
+    else PlBlock<CT, S + PL_S_STEP, SMAX>::run(s, row, base, step, Ms);
   }
 };
 template <typename CT, int SMAX>
-struct PlBlock<CT, SMAX + 1, SMAX> {
+struct PlBlock<CT, SMAX + PL_S_STEP, SMAX> {
   __device__ __forceinline__ static void run(int, CT*, int, int, const CT*) {}
 };
 
@@ -234,12 +252,12 @@ __device__ __forceinline__ void pl_apply_tile(CT* T, const CT* Ms, const PlaneGe
   for (int it = g.warp_start[warp]; it < g.warp_start[warp + 1]; ++it) {
     const int item = g.items[it];
     const int y = item >> 4, col = (item & 15) * 32 + lane;
-    if (col < tcv) PlBlock<CT, 1, SMAX>::run(g.s[y], T + col * g.EP, g.base[y], g.step[y], Ms + g.ms_off[y]);
+    if (col < tcv) PlBlock<CT, PL_S_STEP, SMAX>::run(g.s[y], T + col * g.EP, g.base[y], g.step[y], Ms + g.ms_off[y]);
   }
 }
 
 template <typename CT, int SMAX>
-__global__ void __launch_bounds__(PL_THREADS, 2)
+__global__ void __launch_bounds__(PL_THREADS, (sizeof(CT) == 8 && SMAX <= 12) ? 3 : 2)
     plane_apply_kernel(const CT* __restrict__ in, CT* __restrict__ out, const __grid_constant__ PlaneGeom g,
                        const double2* __restrict__ mat, int mflags, BatchArg bt) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -481,11 +499,11 @@ int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, i
       }
     }
     g.ms_off[y] = ms;
-    ms += g.s[y] * g.s[y];
+    ms += pl_pad(g.s[y]) * pl_pad(g.s[y]);
+    g.nent += g.s[y] * g.s[y];
   }
   g.ms_off[g.nblk] = ms;
   g.ms_total = ms;
-  g.nent = ms;
   // C pass: PL_RT x PL_RT sub-blocks of every block's C, times G column
   // groups when there are few sub-blocks
   g.ncitems = 0;
@@ -513,7 +531,7 @@ int make_plane_geom(int dtype, const AxisView& v, int D, int layout, int swap, i
   const int ncg = (g.TC + 31) / 32;
   std::vector<std::pair<int, int>> items;  // (cost, item)
   for (int y = 0; y < g.nblk; ++y)
-    for (int c = 0; c < ncg; ++c) items.push_back({g.s[y] * g.s[y], (y << 4) | c});
+    for (int c = 0; c < ncg; ++c) items.push_back({pl_pad(g.s[y]) * pl_pad(g.s[y]), (y << 4) | c});
   if ((int)items.size() > PL_MAX_ITEMS) return 0;
   std::stable_sort(items.begin(), items.end(), [](const std::pair<int, int>& a, const std::pair<int, int>& b) {
     return a.first > b.first;
