@@ -243,7 +243,7 @@ __device__ __forceinline__ void adjoint_body(const CT* __restrict__ psi_in, cons
     }
     cp_async_wait_all();  // and its psi_in column
     __syncthreads();  // every thread's column of tile t has landed
-#pragma unroll 2
+#pragma unroll 4
     for (int step = 0; step < TILE / NG; ++step) {
       const int col = step * NG + grp;
       CT lv[RR], pv[RR];
